@@ -1,0 +1,694 @@
+// Host side of guanaco_gb300: error state, FFT twiddle cache, the whole-series
+// FBP plan and every C ABI entry point declared in include/guanaco_gb300.h.
+//
+// The host geometry (per-tilt cos/sin/offset/scale, slab scale/offset) is
+// computed with the reference's float arithmetic; this file is compiled with
+// -ffp-contract=off so the host compiler forms no fused multiply-add on any
+// architecture.
+#include <math.h>
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/guanaco_gb300.h"
+#include "gnc_common.cuh"
+
+namespace gnc {
+
+// ---------------------------------------------------------------- errors ---
+static thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+const char *last_error() { return g_last_error.c_str(); }
+
+// ----------------------------------------------------------- FFT plans -----
+static std::mutex g_fft_lock;
+static std::map<std::pair<int, int>, const float2 *> g_roots;
+
+static bool factorize(long n, int *radix, int *nstage) {
+  int ns = 0;
+  while (n % 8 == 0) { radix[ns++] = 8; n /= 8; }
+  while (n % 4 == 0) { radix[ns++] = 4; n /= 4; }
+  while (n % 2 == 0) { radix[ns++] = 2; n /= 2; }
+  for (long p = 3; n > 1; p += 2) {
+    while (n % p == 0) {
+      if (p > kMaxRadix || ns >= kMaxStages) return false;
+      radix[ns++] = (int)p;
+      n /= p;
+    }
+  }
+  *nstage = ns;
+  return true;
+}
+
+bool fft_length_supported(long n) {
+  int r[kMaxStages], ns = 0;
+  return n >= 1 && factorize(n, r, &ns);
+}
+
+bool make_fft_plan(int n, FftPlan *out) {
+  FftPlan p{};
+  p.n = n;
+  if (!factorize(n, p.radix, &p.nstage)) {
+    set_error("transform length " + std::to_string(n) + " has a prime factor above " +
+              std::to_string(kMaxRadix));
+    return false;
+  }
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(g_fft_lock);
+  auto key = std::make_pair(dev, n);
+  auto it = g_roots.find(key);
+  if (it == g_roots.end()) {
+    std::vector<float2> h(n);
+    for (int k = 0; k < n; ++k) {
+      double a = 2.0 * M_PI * (double)k / (double)n;
+      h[k] = make_float2((float)std::cos(a), (float)-std::sin(a));
+    }
+    float2 *d = nullptr;
+    if (cudaMalloc(&d, n * sizeof(float2)) != cudaSuccess ||
+        cudaMemcpy(d, h.data(), n * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess) {
+      set_error("cannot allocate FFT twiddles");
+      return false;
+    }
+    it = g_roots.emplace(key, d).first;
+  }
+  p.roots = it->second;
+  *out = p;
+  return true;
+}
+
+// ------------------------------------------------------- host geometry -----
+// reconstructor.cpp:35-47 (float arithmetic, std::cos/std::sin of float).
+static TiltGeom tilt_geometry(float theta, float centre, size_t num_angles, float *offset) {
+  double output_scale = M_PI / (double)(2 * num_angles);
+  float cos_angle = std::cos(theta);
+  float sin_angle = std::sin(theta);
+  float det_x0 = -centre * cos_angle;
+  float det_y0 = -centre * sin_angle;
+  float ray_length = std::sqrt(cos_angle * cos_angle + sin_angle * sin_angle);
+  float d = cos_angle * cos_angle + sin_angle * sin_angle;
+  TiltGeom g;
+  *offset = (det_y0 * (-sin_angle) - det_x0 * cos_angle) / d;
+  g.scale = (float)(output_scale * ray_length / std::abs(d));
+  g.cos_a = cos_angle / d;
+  g.sin_a = sin_angle / d;
+  g.pad = 0.f;
+  return g;
+}
+
+// reconstructor.cpp:28-32 / reconstructor.cu:253-256
+static void defocus_scale(size_t num_defocus, float pixel_size, float min_defocus,
+                          float max_defocus, float *dscale, float *doffset) {
+  float ds = num_defocus > 1 ? (float)num_defocus * pixel_size / (max_defocus - min_defocus) : 0.0f;
+  *dscale = ds;
+  *doffset = -ds * (min_defocus / pixel_size);
+}
+
+}  // namespace gnc
+
+using namespace gnc;
+
+#define GNC_REQUIRE(cond)                                                   \
+  do {                                                                      \
+    if (!(cond)) {                                                          \
+      set_error(std::string(__func__) + ": ASSERT (" #cond ") failed");     \
+      return GNC_ERR_INVALID_ARGUMENT;                                      \
+    }                                                                       \
+  } while (0)
+
+#define GNC_CUDA(expr)                                                       \
+  do {                                                                       \
+    cudaError_t e_ = (expr);                                                 \
+    if (e_ != cudaSuccess) {                                                 \
+      set_error(std::string(__func__) + ": " #expr ": " + cudaGetErrorString(e_)); \
+      return e_ == cudaErrorMemoryAllocation ? GNC_ERR_OUT_OF_MEMORY : GNC_ERR_CUDA; \
+    }                                                                        \
+  } while (0)
+
+// ------------------------------------------------------------- the plan ----
+struct gnc_fbp_plan {
+  int device = 0;
+  int T = 0, H = 0, W = 0, Z = 0, X = 0, D = 1, Y2 = 0;
+  int input = GNC_INPUT_RAW, correct = 0, staging = GNC_STAGE_F32;
+  float pixel_size = 1.f, min_def = 0.f, max_def = 0.f, dscale = 0.f, doffset = 0.f;
+  bool uniform_centre = true;
+  int chunk = 1;
+  SignTableArgs sargs{};
+  // device memory
+  float2 *spec = nullptr;   // (T, H, W/2)
+  float2 *gbuf = nullptr;   // (chunk, D, H, W/2)
+  void *staged = nullptr;   // (Y2, D, T, W) pairs
+  int8_t *row_exp = nullptr;
+  int8_t *sign = nullptr;   // (D, H, W/2 + 1)
+  double *slab_df = nullptr;
+  TiltGeom *geom = nullptr;
+  float *offset = nullptr;  // (H, T)
+  float *tilt_factor = nullptr;
+  size_t bytes = 0;
+};
+
+static void plan_free(gnc_fbp_plan *p) {
+  cudaFree(p->spec);
+  cudaFree(p->gbuf);
+  cudaFree(p->staged);
+  cudaFree(p->row_exp);
+  cudaFree(p->sign);
+  cudaFree(p->slab_df);
+  cudaFree(p->geom);
+  cudaFree(p->offset);
+  cudaFree(p->tilt_factor);
+}
+
+template <typename T>
+static cudaError_t dalloc(gnc_fbp_plan *p, T **ptr, size_t count) {
+  size_t b = std::max<size_t>(count, 1) * sizeof(T);
+  p->bytes += b;
+  return cudaMalloc((void **)ptr, b);
+}
+
+static BpArgs bp_args(const gnc_fbp_plan *p, float *vol) {
+  BpArgs a{};
+  a.staged = p->staged;
+  a.row_exp = p->row_exp;
+  a.staging = p->staging;
+  a.Y = p->H;
+  a.D = p->D;
+  a.T = p->T;
+  a.N = p->W;
+  a.Z = p->Z;
+  a.X = p->X;
+  a.geom = p->geom;
+  a.offset = p->offset;
+  a.dscale = p->dscale;
+  a.doffset = p->doffset;
+  a.uniform_centre = p->uniform_centre ? 1 : 0;
+  a.vol = vol;
+  return a;
+}
+
+extern "C" {
+
+const char *gnc_last_error(void) { return last_error(); }
+int gnc_version(void) { return 100; }
+
+int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
+  GNC_REQUIRE(d != nullptr && out != nullptr);
+  *out = nullptr;
+  GNC_REQUIRE(d->num_angles > 0);
+  GNC_REQUIRE(d->height > 0);
+  GNC_REQUIRE(d->width > 0);
+  GNC_REQUIRE(d->grid_height > 0);
+  GNC_REQUIRE(d->grid_width > 0);
+  GNC_REQUIRE(d->pixel_size > 0);
+  GNC_REQUIRE(d->num_defocus > 0);
+  GNC_REQUIRE(d->angles != nullptr);
+  GNC_REQUIRE(d->min_defocus <= d->max_defocus);
+  GNC_REQUIRE(d->num_defocus == 1 || d->max_defocus > d->min_defocus);
+  GNC_REQUIRE(d->input == GNC_INPUT_RAW || d->input == GNC_INPUT_CORRECTED);
+  GNC_REQUIRE(d->staging == GNC_STAGE_F32 || d->staging == GNC_STAGE_F16);
+  const bool ctf = d->input == GNC_INPUT_RAW && d->correct;
+  GNC_REQUIRE(ctf || d->input == GNC_INPUT_CORRECTED || d->num_defocus == 1);
+  if (ctf) GNC_REQUIRE(d->slab_defocus != nullptr);
+  if (d->width > 6400 || !fft_length_supported(2 * (long)d->width) ||
+      (ctf && (d->width % 2 != 0 || d->height > 8192 || !fft_length_supported((long)d->height) ||
+               !fft_length_supported((long)d->width)))) {
+    set_error("gnc_fbp_plan_create: unsupported size (width <= 6400 with 2*width "
+              "factorising into radices <= 16; with CTF correction an even width and a "
+              "height <= 8192 that also factorise)");
+    return GNC_ERR_UNSUPPORTED;
+  }
+  auto *p = new gnc_fbp_plan();
+  cudaGetDevice(&p->device);
+  p->T = (int)d->num_angles;
+  p->H = (int)d->height;
+  p->W = (int)d->width;
+  p->Z = (int)d->grid_height;
+  p->X = (int)d->grid_width;
+  p->D = (int)d->num_defocus;
+  p->Y2 = (p->H + 1) / 2;
+  p->input = d->input;
+  p->correct = ctf ? 1 : 0;
+  p->staging = d->staging;
+  p->pixel_size = d->pixel_size;
+  p->min_def = d->num_defocus > 1 ? d->min_defocus : 0.f;
+  p->max_def = d->num_defocus > 1 ? d->max_defocus : 0.f;
+  defocus_scale(d->num_defocus, d->pixel_size, p->min_def, p->max_def, &p->dscale, &p->doffset);
+
+  // geometry tables
+  std::vector<TiltGeom> geom(p->T);
+  std::vector<float> offset((size_t)p->H * p->T);
+  std::vector<float> centre(p->H);
+  for (int y = 0; y < p->H; ++y) centre[y] = d->centre ? d->centre[y] : (float)(p->W * 0.5);
+  for (int y = 1; y < p->H; ++y)
+    if (centre[y] != centre[0]) p->uniform_centre = false;
+  for (int y = 0; y < p->H; ++y)
+    for (int t = 0; t < p->T; ++t)
+      geom[t] = tilt_geometry(d->angles[t], centre[y], d->num_angles, &offset[(size_t)y * p->T + t]);
+  std::vector<float> factor;
+  if (d->weights || d->minus) {
+    factor.resize(p->T);
+    for (int t = 0; t < p->T; ++t)
+      factor[t] = (float)((d->minus ? -1.0 : 1.0) * (d->weights ? d->weights[t] : 1.0));
+  }
+
+  const size_t half = (size_t)p->W / 2;
+  cudaError_t e = cudaSuccess;
+  if (ctf) {
+    size_t per_tilt = (size_t)p->D * p->H * half * sizeof(float2);
+    p->chunk = (int)std::max<size_t>(1, std::min<size_t>(p->T, (48ull << 20) / per_tilt));
+    if (e == cudaSuccess) e = dalloc(p, &p->spec, (size_t)p->T * p->H * half);
+    if (e == cudaSuccess) e = dalloc(p, &p->gbuf, (size_t)p->chunk * p->D * p->H * half);
+    if (e == cudaSuccess) e = dalloc(p, &p->sign, (size_t)p->D * p->H * (half + 1));
+    if (e == cudaSuccess) e = dalloc(p, &p->slab_df, (size_t)p->D);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(p->slab_df, d->slab_defocus, p->D * sizeof(double), cudaMemcpyHostToDevice);
+    p->sargs.D = p->D;
+    p->sargs.H = p->H;
+    p->sargs.W = p->W;
+    p->sargs.inv_ps = 1.0 / (double)d->pixel_size;
+    p->sargs.l = gnc_get_electron_wavelength(d->energy_kev * 1000);
+    p->sargs.Cs = d->cs_mm * 1e7;
+    p->sargs.Ca = d->astigmatism;
+    p->sargs.Pa = d->astigmatism_angle_deg * M_PI / 180;
+    p->sargs.phi = d->phase_shift_deg * M_PI / 180;
+    p->sargs.slab_df = p->slab_df;
+  }
+  const size_t elems = (size_t)p->Y2 * p->D * p->T * p->W;
+  if (e == cudaSuccess)
+    e = p->staging == GNC_STAGE_F16 ? dalloc(p, (__half2 **)&p->staged, elems)
+                                    : dalloc(p, (float2 **)&p->staged, elems);
+  if (e == cudaSuccess && p->staging == GNC_STAGE_F16)
+    e = dalloc(p, &p->row_exp, (size_t)p->Y2 * p->D * p->T * 2);
+  if (e == cudaSuccess) e = dalloc(p, &p->geom, (size_t)p->T);
+  if (e == cudaSuccess) e = dalloc(p, &p->offset, offset.size());
+  if (e == cudaSuccess)
+    e = cudaMemcpy(p->geom, geom.data(), geom.size() * sizeof(TiltGeom), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(p->offset, offset.data(), offset.size() * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !factor.empty()) {
+    e = dalloc(p, &p->tilt_factor, factor.size());
+    if (e == cudaSuccess)
+      e = cudaMemcpy(p->tilt_factor, factor.data(), factor.size() * sizeof(float),
+                     cudaMemcpyHostToDevice);
+  }
+  if (e != cudaSuccess) {
+    set_error(std::string("gnc_fbp_plan_create: ") + cudaGetErrorString(e));
+    plan_free(p);
+    delete p;
+    return e == cudaErrorMemoryAllocation ? GNC_ERR_OUT_OF_MEMORY : GNC_ERR_CUDA;
+  }
+  *out = p;
+  return GNC_OK;
+}
+
+int gnc_fbp_plan_destroy(gnc_fbp_plan *p) {
+  if (!p) return GNC_OK;
+  plan_free(p);
+  delete p;
+  return GNC_OK;
+}
+
+size_t gnc_fbp_workspace_bytes(const gnc_fbp_plan *p) { return p ? p->bytes : 0; }
+
+int gnc_fbp_sign_table(gnc_fbp_plan *p, int8_t *d_out, void *stream) {
+  GNC_REQUIRE(p != nullptr && p->correct);
+  cudaStream_t s = (cudaStream_t)stream;
+  GNC_CUDA(launch_sign_table(p->sargs, d_out ? d_out : p->sign, s));
+  return GNC_OK;
+}
+
+// Raw or corrected input -> staged filtered rows (the plan's staging buffer).
+int gnc_fbp_stage(gnc_fbp_plan *p, const float *d_input, void *stream) {
+  GNC_REQUIRE(p != nullptr && d_input != nullptr);
+  cudaStream_t s = (cudaStream_t)stream;
+  RowStageArgs r{};
+  r.D = p->D;
+  r.H = p->H;
+  r.N = p->W;
+  r.T = p->T;
+  r.ramp = 1;
+  r.tilt_factor = p->tilt_factor;
+  r.out_staged = 1;
+  r.staging = p->staging;
+  r.staged = p->staged;
+  r.row_exp = p->row_exp;
+  if (p->correct) {
+    GNC_CUDA(launch_sign_table(p->sargs, p->sign, s));
+    GNC_CUDA(launch_rfft_rows(d_input, p->spec, p->T, p->H, p->W, s));
+    GNC_CUDA(launch_column_fft(p->spec, p->T, p->H, p->W, s));
+    r.input_spectra = 1;
+    r.g = p->gbuf;
+    for (int t0 = 0; t0 < p->T; t0 += p->chunk) {
+      int nt = std::min(p->chunk, p->T - t0);
+      GNC_CUDA(launch_column_flip(p->spec, p->gbuf, p->sign, t0, nt, p->D, p->H, p->W, s));
+      r.nt = nt;
+      r.t0 = t0;
+      GNC_CUDA(launch_row_stage(r, s));
+    }
+  } else {
+    r.input_spectra = 0;
+    r.rows = d_input;
+    r.row_stride = p->W;
+    r.plane_stride = (long)p->H * p->W;
+    r.nt = p->T;
+    r.t0 = 0;
+    GNC_CUDA(launch_row_stage(r, s));
+  }
+  return GNC_OK;
+}
+
+int gnc_fbp_backproject(gnc_fbp_plan *p, float *d_volume, int exact, void *stream) {
+  GNC_REQUIRE(p != nullptr && d_volume != nullptr);
+  cudaStream_t s = (cudaStream_t)stream;
+  BpArgs a = bp_args(p, d_volume);
+  if (exact || !p->uniform_centre)
+    GNC_CUDA(launch_backproject_exact(a, s));
+  else
+    GNC_CUDA(launch_backproject_fast(a, s));
+  return GNC_OK;
+}
+
+int gnc_fbp_backproject_staged(gnc_fbp_plan *p, const void *d_staged, const int8_t *d_row_exp,
+                               float *d_volume, int exact, void *stream) {
+  GNC_REQUIRE(p != nullptr && d_staged != nullptr && d_volume != nullptr);
+  GNC_REQUIRE(p->staging != GNC_STAGE_F16 || d_row_exp != nullptr);
+  cudaStream_t s = (cudaStream_t)stream;
+  BpArgs a = bp_args(p, d_volume);
+  a.staged = d_staged;
+  a.row_exp = d_row_exp;
+  if (exact || !p->uniform_centre)
+    GNC_CUDA(launch_backproject_exact(a, s));
+  else
+    GNC_CUDA(launch_backproject_fast(a, s));
+  return GNC_OK;
+}
+
+int gnc_fbp_execute(gnc_fbp_plan *p, const float *d_input, float *d_volume, void *stream) {
+  int st = gnc_fbp_stage(p, d_input, stream);
+  if (st != GNC_OK) return st;
+  return gnc_fbp_backproject(p, d_volume, 0, stream);
+}
+
+int gnc_fbp_execute_host(gnc_fbp_plan *p, const float *h_input, float *h_volume, void *stream) {
+  GNC_REQUIRE(p != nullptr && h_input != nullptr && h_volume != nullptr);
+  cudaStream_t s = (cudaStream_t)stream;
+  size_t in_elems = (size_t)p->T * (p->input == GNC_INPUT_CORRECTED ? p->D : 1) * p->H * p->W;
+  size_t out_elems = (size_t)p->H * p->Z * p->X;
+  float *din = nullptr, *dout = nullptr;
+  GNC_CUDA(cudaMallocAsync((void **)&din, in_elems * sizeof(float), s));
+  cudaError_t e = cudaMallocAsync((void **)&dout, out_elems * sizeof(float), s);
+  if (e != cudaSuccess) {
+    cudaFreeAsync(din, s);
+    GNC_CUDA(e);
+  }
+  int st = GNC_OK;
+  e = cudaMemcpyAsync(din, h_input, in_elems * sizeof(float), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) st = gnc_fbp_execute(p, din, dout, stream);
+  if (e == cudaSuccess && st == GNC_OK)
+    e = cudaMemcpyAsync(h_volume, dout, out_elems * sizeof(float), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(din, s);
+  cudaFreeAsync(dout, s);
+  cudaError_t e2 = cudaStreamSynchronize(s);
+  if (st != GNC_OK) return st;
+  GNC_CUDA(e);
+  GNC_CUDA(e2);
+  return GNC_OK;
+}
+
+int gnc_fbp_correct(gnc_fbp_plan *p, const float *d_proj, float *d_corrected, void *stream) {
+  GNC_REQUIRE(p != nullptr && p->correct && d_proj != nullptr && d_corrected != nullptr);
+  cudaStream_t s = (cudaStream_t)stream;
+  GNC_CUDA(launch_sign_table(p->sargs, p->sign, s));
+  GNC_CUDA(launch_rfft_rows(d_proj, p->spec, p->T, p->H, p->W, s));
+  GNC_CUDA(launch_column_fft(p->spec, p->T, p->H, p->W, s));
+  RowStageArgs r{};
+  r.input_spectra = 1;
+  r.g = p->gbuf;
+  r.D = p->D;
+  r.H = p->H;
+  r.N = p->W;
+  r.T = p->T;
+  r.ramp = 0;
+  r.out_staged = 0;
+  for (int t0 = 0; t0 < p->T; t0 += p->chunk) {
+    int nt = std::min(p->chunk, p->T - t0);
+    GNC_CUDA(launch_column_flip(p->spec, p->gbuf, p->sign, t0, nt, p->D, p->H, p->W, s));
+    r.nt = nt;
+    r.t0 = t0;
+    r.out_rows = d_corrected + (size_t)t0 * p->D * p->H * p->W;
+    GNC_CUDA(launch_row_stage(r, s));
+  }
+  return GNC_OK;
+}
+
+int gnc_fbp_slab_map(gnc_fbp_plan *p, int32_t *d_out, void *stream) {
+  GNC_REQUIRE(p != nullptr && d_out != nullptr);
+  BpArgs a = bp_args(p, nullptr);
+  GNC_CUDA(launch_slab_map(a, d_out, (cudaStream_t)stream));
+  return GNC_OK;
+}
+
+int gnc_fbp_staged(gnc_fbp_plan *p, const void **d_staged, const int8_t **d_row_exp) {
+  GNC_REQUIRE(p != nullptr && d_staged != nullptr);
+  *d_staged = p->staged;
+  if (d_row_exp) *d_row_exp = p->row_exp;
+  return GNC_OK;
+}
+
+// ---------------------------------------------- reference-shaped entry points
+static int select_device(int gpu_index) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    set_error("no CUDA device is available for the device path");
+    return GNC_ERR_DEVICE;
+  }
+  if (gpu_index >= 0) GNC_CUDA(cudaSetDevice(gpu_index));
+  return GNC_OK;
+}
+
+static int check_config(const gnc_config *c) {
+  GNC_REQUIRE(c != nullptr);
+  if (c->device != 1) {
+    set_error("guanaco_gb300 implements the device path (device = gpu) only");
+    return GNC_ERR_UNSUPPORTED;
+  }
+  // Config::is_valid (config.h:66-75)
+  GNC_REQUIRE(c->num_pixels > 0);
+  GNC_REQUIRE(c->num_angles > 0);
+  GNC_REQUIRE(c->num_defocus > 0);
+  GNC_REQUIRE(c->grid_height > 0);
+  GNC_REQUIRE(c->grid_width > 0);
+  GNC_REQUIRE(c->pixel_size > 0);
+  GNC_REQUIRE(c->min_defocus <= c->max_defocus);
+  GNC_REQUIRE(c->angles != nullptr);
+  // BP::launch (reconstructor.cu:250)
+  GNC_REQUIRE(c->num_defocus == 1 || c->max_defocus > c->min_defocus);
+  if (c->num_pixels > 6400 || !fft_length_supported(2 * (long)c->num_pixels)) {
+    set_error("unsupported num_pixels: 2 * num_pixels must factorise into radices <= 16 "
+              "and num_pixels <= 6400");
+    return GNC_ERR_UNSUPPORTED;
+  }
+  return GNC_OK;
+}
+
+int gnc_filter_device(size_t num_pixels, size_t num_angles, size_t num_defocus, float *d_data,
+                      void *stream) {
+  // Filter<e_device>::Filter asserts (filter.cu:139-141)
+  GNC_REQUIRE(num_pixels > 0);
+  GNC_REQUIRE(num_angles > 0);
+  GNC_REQUIRE(num_defocus > 0);
+  GNC_REQUIRE(d_data != nullptr);
+  if (num_pixels > 6400 || !fft_length_supported(2 * (long)num_pixels)) {
+    set_error("unsupported num_pixels for the ramp filter");
+    return GNC_ERR_UNSUPPORTED;
+  }
+  RowStageArgs r{};
+  r.input_spectra = 0;
+  r.rows = d_data;
+  r.row_stride = (long)num_pixels;
+  r.plane_stride = 0;
+  r.nt = 1;
+  r.t0 = 0;
+  r.T = 1;
+  r.D = 1;
+  r.H = (int)(num_angles * num_defocus);
+  r.N = (int)num_pixels;
+  r.ramp = 1;
+  r.out_staged = 0;
+  r.out_rows = d_data;
+  GNC_CUDA(launch_row_stage(r, (cudaStream_t)stream));
+  return GNC_OK;
+}
+
+int gnc_reconstruct_device(const gnc_config *c, const float *d_sino, float *d_rec, void *stream) {
+  int st = check_config(c);
+  if (st != GNC_OK) return st;
+  GNC_REQUIRE(d_sino != nullptr && d_rec != nullptr);
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t sino = c->num_pixels * c->num_angles * c->num_defocus;
+  std::vector<TiltGeom> geom(c->num_angles);
+  float offset = 0.f;
+  for (size_t t = 0; t < c->num_angles; ++t)
+    geom[t] = tilt_geometry(c->angles[t], c->centre, c->num_angles, &offset);
+  float dscale, doffset;
+  defocus_scale(c->num_defocus, c->pixel_size, c->min_defocus, c->max_defocus, &dscale, &doffset);
+  float *filtered = nullptr;
+  TiltGeom *dgeom = nullptr;
+  GNC_CUDA(cudaMallocAsync((void **)&filtered, sino * sizeof(float), s));
+  cudaError_t e = cudaMallocAsync((void **)&dgeom, geom.size() * sizeof(TiltGeom), s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dgeom, geom.data(), geom.size() * sizeof(TiltGeom),
+                        cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(filtered, d_sino, sino * sizeof(float), cudaMemcpyDeviceToDevice, s);
+  int rc = GNC_OK;
+  if (e == cudaSuccess)
+    rc = gnc_filter_device(c->num_pixels, c->num_angles, c->num_defocus, filtered, stream);
+  if (e == cudaSuccess && rc == GNC_OK) {
+    SliceBpArgs a{};
+    a.sino = filtered;
+    a.D = (int)c->num_defocus;
+    a.T = (int)c->num_angles;
+    a.N = (int)c->num_pixels;
+    a.Z = (int)c->grid_height;
+    a.X = (int)c->grid_width;
+    a.geom = dgeom;
+    a.offset = offset;
+    a.dscale = dscale;
+    a.doffset = doffset;
+    a.rec = d_rec;
+    e = launch_backproject_slice(a, s);
+  }
+  cudaFreeAsync(filtered, s);
+  cudaFreeAsync(dgeom, s);
+  if (rc != GNC_OK) return rc;
+  GNC_CUDA(e);
+  return GNC_OK;
+}
+
+int gnc_reconstruct(const gnc_config *c, const float *sinogram, float *reconstruction) {
+  int st = check_config(c);
+  if (st != GNC_OK) return st;
+  GNC_REQUIRE(sinogram != nullptr && reconstruction != nullptr);
+  st = select_device(c->gpu_index);
+  if (st != GNC_OK) return st;
+  const size_t sino = c->num_pixels * c->num_angles * c->num_defocus;
+  const size_t grid = c->grid_height * c->grid_width;
+  cudaStream_t s = nullptr;
+  float *ds = nullptr, *dr = nullptr;
+  GNC_CUDA(cudaMallocAsync((void **)&ds, sino * sizeof(float), s));
+  cudaError_t e = cudaMallocAsync((void **)&dr, grid * sizeof(float), s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(ds, sinogram, sino * sizeof(float), cudaMemcpyHostToDevice, s);
+  int rc = GNC_OK;
+  if (e == cudaSuccess) rc = gnc_reconstruct_device(c, ds, dr, s);
+  if (e == cudaSuccess && rc == GNC_OK)
+    e = cudaMemcpyAsync(reconstruction, dr, grid * sizeof(float), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(ds, s);
+  cudaFreeAsync(dr, s);
+  cudaError_t e2 = cudaStreamSynchronize(s);
+  if (rc != GNC_OK) return rc;
+  GNC_CUDA(e);
+  GNC_CUDA(e2);
+  return GNC_OK;
+}
+
+// Phase-flip table straight from a complex64 CTF stack: s = -sign(imag),
+// stored symmetrised as s(k) + s(-k) for kx <= W/2 (correct.h:30-39).
+__global__ void k_sign_from_ctf(const float2 *__restrict__ ctf, int D, int H, int W,
+                                int8_t *__restrict__ out) {
+  const int half = W / 2, sw = half + 1;
+  const long total = (long)D * H * sw;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total;
+       i += (long)gridDim.x * blockDim.x) {
+    int kx = (int)(i % sw);
+    long r = i / sw;
+    int ky = (int)(r % H);
+    int d = (int)(r / H);
+    const float2 *c = ctf + (size_t)d * H * W;
+    float a = c[(size_t)ky * W + kx].y;
+    float b = c[(size_t)((H - ky) % H) * W + (W - kx) % W].y;
+    int sa = -((0.0f < a) - (a < 0.0f));
+    int sb = -((0.0f < b) - (b < 0.0f));
+    out[i] = (int8_t)(sa + sb);
+  }
+}
+
+int gnc_correct(const float *image, const float *ctf, float *rec, size_t xsize, size_t ysize,
+                size_t num_ctf) {
+  // Corrector::correct asserts (correct.cu:38-40)
+  GNC_REQUIRE(xsize > 0);
+  GNC_REQUIRE(ysize > 0);
+  GNC_REQUIRE(num_ctf > 0);
+  GNC_REQUIRE(image != nullptr && ctf != nullptr && rec != nullptr);
+  if (xsize % 2 != 0 || ysize > 8192 || xsize > 16384 || !fft_length_supported((long)xsize) ||
+      !fft_length_supported((long)ysize)) {
+    set_error("gnc_correct: unsupported image size (even width; width and height must "
+              "factorise into radices <= 16; height <= 8192)");
+    return GNC_ERR_UNSUPPORTED;
+  }
+  int st = select_device(-1);
+  if (st != GNC_OK) return st;
+  const int W = (int)xsize, H = (int)ysize, D = (int)num_ctf;
+  const size_t img = xsize * ysize, half = xsize / 2;
+  cudaStream_t s = nullptr;
+  float *dimg = nullptr, *drec = nullptr;
+  float2 *dctf = nullptr, *spec = nullptr, *g = nullptr;
+  int8_t *sign = nullptr;
+  auto release = [&]() {
+    cudaFreeAsync(dimg, s);
+    cudaFreeAsync(drec, s);
+    cudaFreeAsync(dctf, s);
+    cudaFreeAsync(spec, s);
+    cudaFreeAsync(g, s);
+    cudaFreeAsync(sign, s);
+  };
+  cudaError_t e = cudaMallocAsync((void **)&dimg, img * sizeof(float), s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void **)&drec, D * img * sizeof(float), s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void **)&dctf, D * img * sizeof(float2), s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void **)&spec, H * half * sizeof(float2), s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void **)&g, D * H * half * sizeof(float2), s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void **)&sign, D * H * (half + 1), s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dimg, image, img * sizeof(float), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dctf, ctf, D * img * sizeof(float2), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    k_sign_from_ctf<<<std::min<long>(4096, ((long)D * H * (half + 1) + 255) / 256), 256, 0, s>>>(
+        dctf, D, H, W, sign);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = launch_rfft_rows(dimg, spec, 1, H, W, s);
+  if (e == cudaSuccess) e = launch_column_fft(spec, 1, H, W, s);
+  if (e == cudaSuccess) e = launch_column_flip(spec, g, sign, 0, 1, D, H, W, s);
+  if (e == cudaSuccess) {
+    RowStageArgs r{};
+    r.input_spectra = 1;
+    r.g = g;
+    r.nt = 1;
+    r.t0 = 0;
+    r.T = 1;
+    r.D = D;
+    r.H = H;
+    r.N = W;
+    r.ramp = 0;
+    r.out_staged = 0;
+    r.out_rows = drec;
+    e = launch_row_stage(r, s);
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(rec, drec, D * img * sizeof(float), cudaMemcpyDeviceToHost, s);
+  release();
+  cudaError_t e2 = cudaStreamSynchronize(s);
+  GNC_CUDA(e);
+  GNC_CUDA(e2);
+  return GNC_OK;
+}
+
+}  // extern "C"

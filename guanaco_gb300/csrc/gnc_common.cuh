@@ -1,0 +1,138 @@
+// Internal interfaces shared by the guanaco_gb300 CUDA translation units.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "gnc_fft.cuh"
+
+namespace gnc {
+
+// ---- errors -------------------------------------------------------------
+void set_error(const std::string &msg);
+const char *last_error();
+
+// ---- FFT plans: factorisation + device twiddles, cached per (device, n) ---
+// Returns false (and sets the error) when n has a prime factor > kMaxRadix.
+bool make_fft_plan(int n, FftPlan *out);
+bool fft_length_supported(long n);
+
+// ---- staging element types ------------------------------------------------
+enum Staging : int { kStageF32 = 0, kStageF16 = 1 };
+
+// Per-tilt backprojection geometry, computed on the host with the reference's
+// float arithmetic (src/libguanaco/reconstructor.cpp:35-47).
+struct TiltGeom {
+  float cos_a;  // cos(theta) / d
+  float sin_a;  // sin(theta) / d
+  float scale;  // pi / (2 T) * ray_length / |d|
+  float pad;
+};
+
+// ---- kernels (launchers return the launch error) ---------------------------
+
+// Row transform of the raw projections: rows (t, 2p) and (t, 2p+1) are packed
+// as one complex row, transformed and unpacked into two half spectra of W/2
+// bins with the DC and Nyquist real parts packed in bin 0.
+// proj (T, H, W) -> spec (T, H, W/2).
+cudaError_t launch_rfft_rows(const float *proj, float2 *spec, int T, int H, int W,
+                             cudaStream_t s);
+
+// Forward column transform of every tilt's half spectrum, in place.
+cudaError_t launch_column_fft(float2 *spec, int T, int H, int W, cudaStream_t s);
+
+// Per-slab phase flip and inverse column transform for the tilts
+// [t0, t0 + nt) of the column-transformed spectra: spec (T, H, W/2) ->
+// g (nt, D, H, W/2).
+// sign: (D, H, W/2 + 1) int8 holding 2 * (s(k) + s(-k)) / 2.
+cudaError_t launch_column_flip(const float2 *spec, float2 *g, const int8_t *sign, int t0, int nt,
+                               int D, int H, int W, cudaStream_t s);
+
+// The 2 * symmetrised phase-flip sign for every (slab, ky, kx <= W/2), from the
+// FP64 CTF phase (include/guanaco/ctf.h:88-101, 233-273; correct.h:30-39).
+struct SignTableArgs {
+  int D, H, W;
+  double inv_ps;
+  double l, Cs, Ca, Pa, phi;
+  const double *slab_df;  // device, D
+};
+cudaError_t launch_sign_table(const SignTableArgs &a, int8_t *out, cudaStream_t s);
+
+// Row stage.  Input rows come either from the column stage (packed half
+// spectra, INPUT_SPECTRA) or from real rows.  Each pair of rows is one complex
+// row.  With RAMP the rows are zero padded to 2N, ramp filtered
+// (src/libguanaco/filter.cpp:30-97) and divided by 2N; without it they are the
+// corrected rows (correct.cpp:78-84).  Output is either the staged pair layout
+// for the backprojector or plain real rows.
+struct RowStageArgs {
+  // input
+  int input_spectra;     // 1: packed half spectra (G), 0: real rows
+  const float2 *g;       // (nt, D, H, W/2) when input_spectra
+  const float *rows;     // real rows when !input_spectra
+  long row_stride;       // floats between consecutive input rows (y)
+  long plane_stride;     // floats between consecutive (t, d) planes of rows
+  // geometry
+  int nt, D, H, N;       // tilts in this launch, slabs, rows per image, row length
+  int t0;                // first tilt of this launch (into weights/output)
+  int T;                 // total tilts (output layout)
+  int ramp;              // apply the ramp filter
+  // per-tilt factor (weight * sign) or null
+  const float *tilt_factor;
+  // output
+  int out_staged;        // 1: staged pairs (Y2, D, T, N), 0: plain rows
+  int staging;           // kStageF32 / kStageF16 when out_staged
+  void *staged;          // float2 or __half2
+  int8_t *row_exp;       // (Y2, D, T, 2) FP16 exponents when staging == F16
+  float *out_rows;       // plain rows: (nt, D, H, N) at [t][d][y][n]
+};
+cudaError_t launch_row_stage(const RowStageArgs &a, cudaStream_t s);
+
+// Backprojection of the staged pairs into the volume (Y, Z, X).
+struct BpArgs {
+  const void *staged;     // (Y2, D, T, N) float2 / __half2
+  const int8_t *row_exp;  // F16 exponents or null
+  int staging;
+  int Y, D, T, N, Z, X;
+  const TiltGeom *geom;   // T
+  const float *offset;    // (Y, T): detector offset of each row (depends on its centre)
+  float dscale, doffset;  // slab map (reconstructor.cpp:28-32)
+  int uniform_centre;     // all rows share one centre
+  float *vol;             // (Y, Z, X)
+};
+cudaError_t launch_backproject_exact(const BpArgs &a, cudaStream_t s);
+cudaError_t launch_backproject_fast(const BpArgs &a, cudaStream_t s);
+cudaError_t launch_slab_map(const BpArgs &a, int32_t *out, cudaStream_t s);
+
+// Single-slice backprojection of plain filtered rows (D, T, N) into (Z, X):
+// the per-call path of guanaco.detail.recon.
+struct SliceBpArgs {
+  const float *sino;  // (D, T, N)
+  int D, T, N, Z, X;
+  const TiltGeom *geom;
+  float offset;
+  float dscale, doffset;
+  float *rec;          // (Z, X)
+};
+cudaError_t launch_backproject_slice(const SliceBpArgs &a, cudaStream_t s);
+
+// Exact slab index of the reference (reconstructor.cpp:66-72): the height and
+// defocus coordinate in float without contraction, then
+// floor((double)defocus + 0.5) clamped to [0, D-1].  floor(d + 0.5) equals
+// floor(d) + (d - floor(d) >= 0.5); d - floor(d) is exact for d >= 0 (Sterbenz)
+// and any rounding for d in (-1, 0) only moves the result between -1 and 0,
+// which the clamp maps to 0 alike.
+__device__ __forceinline__ int slab_index(float x, float y, float sin_a, float cos_a,
+                                          float dscale, float doffset, int D) {
+  float height = __fsub_rn(__fmul_rn(-x, sin_a), __fmul_rn(y, cos_a));
+  float defocus = __fadd_rn(__fmul_rn(height, dscale), doffset);
+  float fl = floorf(defocus);
+  float fr = __fsub_rn(defocus, fl);
+  int k = (int)fl + (fr >= 0.5f ? 1 : 0);
+  k = k < 0 ? 0 : k;
+  return k > D - 1 ? D - 1 : k;
+}
+
+}  // namespace gnc

@@ -1,0 +1,197 @@
+// CTF physics: the device sign table used by the phase flip and the host
+// functions behind the CTF entry points.  This file is compiled with
+// -fmad=false so that double expressions keep the reference's evaluation order
+// (include/guanaco/ctf.h), without fused multiply-adds.
+#include <math.h>
+
+#include "gnc_common.cuh"
+
+namespace gnc {
+
+// FFT-ordered spatial frequency of bin (x, y): include/guanaco/ctf.h:88-101.
+__host__ __device__ inline void r_and_theta(long x, long y, long w, long h, double inv_ps,
+                                            bool need_theta, double *r, double *theta) {
+  long w2 = w / 2, h2 = h / 2;
+  double dx = ((double)((x + w2) % w) - (double)w2) / (double)w;
+  double dy = ((double)((y + h2) % h) - (double)h2) / (double)h;
+  *r = sqrt((dx * dx + dy * dy) * inv_ps * inv_ps);
+  *theta = need_theta ? atan2(dy, dx) : 0.0;
+}
+
+// chi: include/guanaco/ctf.h:233-238.
+__host__ __device__ inline double chi(double l, double df0, double Cs, double Ca, double Pa,
+                                      double q, double theta) {
+  double df = df0 + Ca * cos(2 * (theta - Pa));
+  return M_PI * (Cs * l * l * l * q * q * q * q / 2 - l * df * q * q);
+}
+
+// The reference stores exp(-i(chi - phi)) as complex64 (correct.py:192-211)
+// and phase_flip multiplies by -sign(imag) (correct.h:30-39).
+__device__ inline int flip_sign(double l, double df, double Cs, double Ca, double Pa, double phi,
+                                long x, long y, long w, long h, double inv_ps) {
+  double q, theta;
+  r_and_theta(x, y, w, h, inv_ps, Ca != 0.0, &q, &theta);
+  double a = -(chi(l, df, Cs, Ca, Pa, q, theta) - phi);
+  float im = (float)sin(a);
+  return -((0.0f < im) - (im < 0.0f));
+}
+
+__global__ void k_sign_table(SignTableArgs a, int8_t *__restrict__ out) {
+  const int half = a.W / 2;
+  const int sw = half + 1;
+  const long total = (long)a.D * a.H * sw;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total;
+       i += (long)gridDim.x * blockDim.x) {
+    int kx = (int)(i % sw);
+    long r = i / sw;
+    int ky = (int)(r % a.H);
+    int d = (int)(r / a.H);
+    double df = a.slab_df[d];
+    int s0 = flip_sign(a.l, df, a.Cs, a.Ca, a.Pa, a.phi, kx, ky, a.W, a.H, a.inv_ps);
+    int s1;
+    if (a.Ca == 0.0) {
+      // without astigmatism q(-k) == q(k) bit for bit, so s(-k) == s(k)
+      s1 = s0;
+    } else {
+      s1 = flip_sign(a.l, df, a.Cs, a.Ca, a.Pa, a.phi, (a.W - kx) % a.W, (a.H - ky) % a.H, a.W,
+                     a.H, a.inv_ps);
+    }
+    out[i] = (int8_t)(s0 + s1);
+  }
+}
+
+cudaError_t launch_sign_table(const SignTableArgs &a, int8_t *out, cudaStream_t s) {
+  long total = (long)a.D * a.H * (a.W / 2 + 1);
+  int blocks = (int)((total + 255) / 256);
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  k_sign_table<<<blocks, 256, 0, s>>>(a, out);
+  return cudaGetLastError();
+}
+
+}  // namespace gnc
+
+// ---------------------------------------------------------------------------
+// Host CTF functions (include/guanaco/ctf.h), exported through the C ABI.
+// ---------------------------------------------------------------------------
+#include "../../include/guanaco_gb300.h"
+
+namespace {
+const double kC = 2.99792458e8;        // constants.h:31
+const double kE = 1.602176634e-19;     // constants.h:32
+const double kMe = 9.1093837015e-31;   // constants.h:33
+const double kH = 6.62607004e-34;      // constants.h:34
+const double kMtoA = 1e10;             // constants.h:35
+
+double log_Es(const gnc_ctf *c, double q, double theta) {  // ctf.h:188-195
+  double df = c->df + c->Ca * cos(2 * (theta - c->Pa));
+  double u = 1 + 2 * M_PI * M_PI * c->theta_c * c->theta_c * c->dd * c->dd * q * q;
+  double v = c->Cs * c->l * c->l * c->l * q * q * q - df * c->l * q;
+  return -(M_PI * M_PI * c->theta_c * c->theta_c * v * v / (c->l * c->l * u));
+}
+double log_Et(const gnc_ctf *c, double q) {  // ctf.h:204-209
+  double u = 1 + 2 * M_PI * M_PI * c->theta_c * c->theta_c * c->dd * c->dd * q * q;
+  return -(M_PI * M_PI * c->l * c->l * c->dd * c->dd * q * q * q * q / (2 * u));
+}
+double env_A(const gnc_ctf *c, double q) {  // ctf.h:218-223
+  double u = 1 + 2 * M_PI * M_PI * c->theta_c * c->theta_c * c->dd * c->dd * q * q;
+  return 1 / sqrt(u);
+}
+}  // namespace
+
+extern "C" {
+
+double gnc_get_electron_wavelength(double V) {  // ctf.h:39-48
+  double eV = kE * V;
+  return (kH * kC / sqrt(eV * eV + 2 * kMe * eV * kC * kC)) * kMtoA;
+}
+
+double gnc_get_defocus_spread(double Cc, double dEE, double dII, double dVV) {  // ctf.h:61-64
+  return Cc * sqrt((dEE) * (dEE) + (2 * dII) * (2 * dII) + (dVV) * (dVV));
+}
+
+double gnc_q_to_Q(double q, double l, double Cs) { return q * pow(Cs * l * l * l, 1.0 / 4.0); }
+double gnc_Q_to_q(double Q, double l, double Cs) { return Q / pow(Cs * l * l * l, 1.0 / 4.0); }
+double gnc_df_to_D(double df, double l, double Cs) { return df / sqrt(Cs * l); }
+double gnc_D_to_df(double D, double l, double Cs) { return D * sqrt(Cs * l); }
+
+double gnc_ctf_chi(const gnc_ctf *c, double q, double theta) {
+  return gnc::chi(c->l, c->df, c->Cs, c->Ca, c->Pa, q, theta);
+}
+
+int gnc_ctf_eval(const gnc_ctf *c, int kind, const double *q, const double *theta, size_t n,
+                 double *out) {
+  if (!c || !q || !out || (!theta && kind != GNC_CTF_ET)) {
+    gnc::set_error("gnc_ctf_eval: null pointer");
+    return GNC_ERR_INVALID_ARGUMENT;
+  }
+  for (size_t i = 0; i < n; ++i) {
+    double qi = q[i], ti = theta ? theta[i] : 0.0;
+    switch (kind) {
+      case GNC_CTF_FULL: {  // ctf.h:250-257
+        double x = gnc::chi(c->l, c->df, c->Cs, c->Ca, c->Pa, qi, ti);
+        double mag = env_A(c, qi) * exp(log_Es(c, qi, ti) + log_Et(c, qi));
+        out[2 * i] = mag * cos(-(x - c->phi));
+        out[2 * i + 1] = mag * sin(-(x - c->phi));
+        break;
+      }
+      case GNC_CTF_SIMPLE: {  // ctf.h:269-273
+        double x = gnc::chi(c->l, c->df, c->Cs, c->Ca, c->Pa, qi, ti);
+        out[2 * i] = cos(-(x - c->phi));
+        out[2 * i + 1] = sin(-(x - c->phi));
+        break;
+      }
+      case GNC_CTF_SIMPLE_REAL:  // ctf.h:285-288
+        out[i] = cos(-(gnc::chi(c->l, c->df, c->Cs, c->Ca, c->Pa, qi, ti) - c->phi));
+        break;
+      case GNC_CTF_SIMPLE_IMAG:  // ctf.h:300-303
+        out[i] = sin(-(gnc::chi(c->l, c->df, c->Cs, c->Ca, c->Pa, qi, ti) - c->phi));
+        break;
+      case GNC_CTF_CHI:
+        out[i] = gnc::chi(c->l, c->df, c->Cs, c->Ca, c->Pa, qi, ti);
+        break;
+      case GNC_CTF_ES:  // ctf.h:314-319
+        out[i] = exp(log_Es(c, qi, ti));
+        break;
+      case GNC_CTF_ET:  // ctf.h:329-332
+        out[i] = exp(log_Et(c, qi));
+        break;
+      default:
+        gnc::set_error("gnc_ctf_eval: unknown kind");
+        return GNC_ERR_INVALID_ARGUMENT;
+    }
+  }
+  return GNC_OK;
+}
+
+int gnc_q_and_theta(size_t w, size_t h, double ps, double *q, double *theta) {
+  if (!(ps > 0) || !q || !theta) {
+    gnc::set_error("gnc_q_and_theta: ps must be > 0 and outputs non-null");
+    return GNC_ERR_INVALID_ARGUMENT;
+  }
+  double inv_ps = 1.0 / ps;
+  for (size_t j = 0; j < h; ++j)
+    for (size_t i = 0; i < w; ++i)
+      gnc::r_and_theta((long)i, (long)j, (long)w, (long)h, inv_ps, true, &q[j * w + i],
+                       &theta[j * w + i]);
+  return GNC_OK;
+}
+
+int gnc_ctf_grid(const gnc_ctf *c, int kind, size_t w, size_t h, double ps, double *out) {
+  if (!c || !out || !(ps > 0)) {  // ctf.h:466-557 assert ps > 0
+    gnc::set_error("gnc_ctf_grid: ps must be > 0 and pointers non-null");
+    return GNC_ERR_INVALID_ARGUMENT;
+  }
+  double inv_ps = 1.0 / ps;
+  int cplx = (kind == GNC_CTF_FULL || kind == GNC_CTF_SIMPLE) ? 2 : 1;
+  for (size_t j = 0; j < h; ++j) {
+    for (size_t i = 0; i < w; ++i) {
+      double q, theta;
+      gnc::r_and_theta((long)i, (long)j, (long)w, (long)h, inv_ps, true, &q, &theta);
+      int st = gnc_ctf_eval(c, kind, &q, &theta, 1, out + cplx * (j * w + i));
+      if (st != GNC_OK) return st;
+    }
+  }
+  return GNC_OK;
+}
+
+}  // extern "C"

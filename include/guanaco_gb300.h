@@ -1,0 +1,210 @@
+/*
+ * guanaco_gb300 -- C ABI of the GB300 (sm_103a) implementation of guanaco's
+ * 3D-CTF filtered-backprojection path.
+ *
+ * Every entry point returns a gnc_status (0 on success).  On failure
+ * gnc_last_error() returns a message for the calling thread; argument checks
+ * that correspond to a GUANACO_ASSERT in the reference report
+ * GNC_ERR_INVALID_ARGUMENT with the asserted condition in the message, the
+ * way guanaco::Error carries "file:line ASSERT (...) failed"
+ * (include/guanaco/error.h:31-61).
+ *
+ * Pointers are plain host or device pointers (as named), sizes are element
+ * counts, streams are cudaStream_t passed as void* (NULL = legacy default
+ * stream).  No entry point takes ownership of caller memory.
+ *
+ * Reference paths below are relative to the guanaco source tree.
+ */
+#ifndef GUANACO_GB300_H
+#define GUANACO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define GNC_API __attribute__((visibility("default")))
+#else
+#define GNC_API
+#endif
+
+typedef enum {
+  GNC_OK = 0,
+  GNC_ERR_INVALID_ARGUMENT = 1, /* a reference GUANACO_ASSERT would fire */
+  GNC_ERR_UNSUPPORTED = 2,      /* valid for the reference, not built here (message says why) */
+  GNC_ERR_CUDA = 3,             /* CUDA runtime error (message has cudaGetErrorString) */
+  GNC_ERR_OUT_OF_MEMORY = 4,
+  GNC_ERR_DEVICE = 5            /* device path requested on a machine without a usable GPU */
+} gnc_status;
+
+/* Message of the last failed call on this thread ("" if none). */
+GNC_API const char *gnc_last_error(void);
+/* ABI version: major * 10000 + minor * 100 + patch. */
+GNC_API int gnc_version(void);
+
+/* ------------------------------------------------------------------------
+ * Configuration: guanaco::Config (include/guanaco/config.h:29-76).
+ * device 1 = e_device is the only value this library runs; 0 = e_host is
+ * rejected with GNC_ERR_UNSUPPORTED (the CPU path is the reference's).
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  int device;           /* eDevice: 0 e_host, 1 e_device */
+  int gpu_index;        /* cudaSetDevice(gpu_index) when >= 0 (reconstructor.cu:321-328) */
+  size_t num_pixels;    /* N */
+  size_t num_angles;    /* T */
+  size_t num_defocus;   /* D */
+  size_t grid_height;   /* Z */
+  size_t grid_width;    /* X */
+  float pixel_size;     /* A */
+  float centre;         /* rotation centre (px) */
+  float min_defocus;    /* A, relative to the defocus at the tilt axis */
+  float max_defocus;    /* A */
+  const float *angles;  /* host, num_angles, radians */
+} gnc_config;
+
+/* guanaco::Reconstructor(config)(sinogram, reconstruction) on the device path
+ * (src/libguanaco/reconstructor.cpp:117-131 -> reconstructor.cu:317-354).
+ * Host pointers: sinogram (D, T, N) float32, reconstruction (Z, X) float32,
+ * overwritten.  Synchronous.  Bound from Python as guanaco.detail.recon
+ * (src/guanaco/detail/ext/reconstruct.h:35-101). */
+GNC_API int gnc_reconstruct(const gnc_config *config, const float *sinogram,
+                            float *reconstruction);
+
+/* The same on device pointers, enqueued on `stream`. */
+GNC_API int gnc_reconstruct_device(const gnc_config *config, const float *d_sinogram,
+                                   float *d_reconstruction, void *stream);
+
+/* guanaco::Filter<e_device>(num_pixels, num_angles, num_defocus)(data)
+ * (include/guanaco/filter.h:32-54, src/libguanaco/filter.cu:144-202): ramp
+ * filter of D*T rows of N pixels in place, device pointer. */
+GNC_API int gnc_filter_device(size_t num_pixels, size_t num_angles, size_t num_defocus,
+                              float *d_data, void *stream);
+
+/* guanaco::correct<float>(image, ctf, rec, xsize, ysize, num_ctf, e_device)
+ * (include/guanaco/correct.h:77-95, src/libguanaco/correct.cu:30-86).
+ * Host pointers: image (ysize, xsize) float32, ctf (num_ctf, ysize, xsize)
+ * complex64 as interleaved float pairs, rec (num_ctf, ysize, xsize) float32.
+ * Output is unnormalised (xsize * ysize times the corrected image), as in the
+ * reference.  Bound from Python as guanaco.detail.corr
+ * (src/guanaco/detail/ext/correct.h:32-76). */
+GNC_API int gnc_correct(const float *image, const float *ctf, float *rec, size_t xsize,
+                        size_t ysize, size_t num_ctf);
+
+/* ------------------------------------------------------------------------
+ * CTF physics, host, double (include/guanaco/ctf.h).  Bound from Python as
+ * the guanaco_ext CTF class and free functions (src/guanaco/detail/ext/ctf.h).
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  double l;       /* wavelength (A) */
+  double df;      /* defocus (A) */
+  double Cs;      /* spherical aberration (A) */
+  double Ca;      /* 2-fold astigmatism (A) */
+  double Pa;      /* astigmatism angle (rad) */
+  double dd;      /* defocus spread (A) */
+  double theta_c; /* source spread (rad) */
+  double phi;     /* phase shift (rad) */
+} gnc_ctf; /* guanaco::CTF, ctf.h:167-178 */
+
+enum {
+  GNC_CTF_FULL = 0,        /* complex: get_ctf, ctf.h:250-257 */
+  GNC_CTF_SIMPLE = 1,      /* complex: get_ctf_simple, ctf.h:269-273 */
+  GNC_CTF_SIMPLE_REAL = 2, /* ctf.h:285-288 */
+  GNC_CTF_SIMPLE_IMAG = 3, /* ctf.h:300-303 */
+  GNC_CTF_CHI = 4,         /* get_chi, ctf.h:233-238 */
+  GNC_CTF_ES = 5,          /* exp(get_log_Es), ctf.h:314-319 */
+  GNC_CTF_ET = 6           /* exp(get_log_Et), ctf.h:329-332 */
+};
+
+GNC_API double gnc_get_electron_wavelength(double V);                       /* ctf.h:39-48 */
+GNC_API double gnc_get_defocus_spread(double Cc, double dEE, double dII, double dVV); /* :61-64 */
+GNC_API double gnc_q_to_Q(double q, double l, double Cs);                   /* ctf.h:114-117 */
+GNC_API double gnc_Q_to_q(double Q, double l, double Cs);                   /* ctf.h:129-132 */
+GNC_API double gnc_df_to_D(double df, double l, double Cs);                 /* ctf.h:144-147 */
+GNC_API double gnc_D_to_df(double D, double l, double Cs);                  /* ctf.h:159-162 */
+GNC_API double gnc_ctf_chi(const gnc_ctf *c, double q, double theta);       /* ctf.h:233-238 */
+/* Element-wise over n (q, theta) pairs; complex kinds write 2n doubles. */
+GNC_API int gnc_ctf_eval(const gnc_ctf *c, int kind, const double *q, const double *theta,
+                         size_t n, double *out);
+/* (h, w) FFT-ordered grid at pixel size ps: ctf.h:466-557; get_q_and_theta
+ * (src/guanaco/detail/ext/ctf.h:41-56). */
+GNC_API int gnc_ctf_grid(const gnc_ctf *c, int kind, size_t w, size_t h, double ps, double *out);
+GNC_API int gnc_q_and_theta(size_t w, size_t h, double ps, double *q, double *theta);
+
+/* ------------------------------------------------------------------------
+ * Whole-series 3D-CTF FBP.  One plan replaces the reference's
+ * correct_projections (src/guanaco/detail/correct.py:217-318, one corr call
+ * per tilt) followed by reconstruct (src/guanaco/detail/reconstruct.py:127-213,
+ * one recon call per Y row from src/guanaco/detail/mp.py:106-153): the same
+ * arithmetic, for every tilt and row in one device-resident pass.
+ * ---------------------------------------------------------------------- */
+typedef struct gnc_fbp_plan gnc_fbp_plan;
+
+enum { GNC_STAGE_F32 = 0, GNC_STAGE_F16 = 1 };
+enum { GNC_INPUT_RAW = 0, GNC_INPUT_CORRECTED = 1 };
+
+typedef struct {
+  size_t num_angles;     /* T */
+  size_t height;         /* H: image rows = volume Y */
+  size_t width;          /* W: image columns = detector pixels N */
+  size_t grid_height;    /* Z (the reference's Python path uses W) */
+  size_t grid_width;     /* X (the reference's Python path uses W) */
+  const float *angles;   /* host, T radians */
+  const float *centre;   /* host, H per-row rotation centres; NULL = W / 2 */
+  float pixel_size;      /* A */
+  int input;             /* GNC_INPUT_RAW: (T, H, W) projections, corrected here;
+                            GNC_INPUT_CORRECTED: (T, D, H, W) already corrected */
+  int correct;           /* RAW input only: 1 = CTF phase flip, 0 = none (D must be 1) */
+  size_t num_defocus;    /* D >= 1 */
+  const double *slab_defocus; /* host, D absolute slab defoci (A) for the CTF (correct.py:195-199) */
+  float min_defocus;     /* relative range handed to the backprojector (correct.py:318) */
+  float max_defocus;
+  double energy_kev;     /* CTF: wavelength from energy * 1000 eV (correct.py:146) */
+  double cs_mm;          /* CTF: Cs * 1e7 A (correct.py:148) */
+  double astigmatism;    /* A */
+  double astigmatism_angle_deg;
+  double phase_shift_deg;
+  const double *weights; /* host, T per-tilt weights (mp.py:135-141) or NULL */
+  int minus;             /* transform == "minus" (mp.py:128-129) */
+  int staging;           /* GNC_STAGE_F32 or GNC_STAGE_F16 */
+} gnc_fbp_desc;
+
+/* Allocates the plan's device workspace on the current device. */
+GNC_API int gnc_fbp_plan_create(const gnc_fbp_desc *desc, gnc_fbp_plan **plan);
+GNC_API int gnc_fbp_plan_destroy(gnc_fbp_plan *plan);
+GNC_API size_t gnc_fbp_workspace_bytes(const gnc_fbp_plan *plan);
+/* Input (T, H, W) or (T, D, H, W) float32 device; volume (H, Z, X) float32
+ * device, overwritten. */
+GNC_API int gnc_fbp_execute(gnc_fbp_plan *plan, const float *d_input, float *d_volume,
+                            void *stream);
+/* The same from host buffers: copies in, executes, copies out, synchronises
+ * the stream.  Pinned host memory gives the fastest copies. */
+GNC_API int gnc_fbp_execute_host(gnc_fbp_plan *plan, const float *h_input, float *h_volume,
+                                 void *stream);
+/* Correction only: raw (T, H, W) -> corrected stack (T, D, H, W), the output
+ * of correct_projections (correct.py:276-303), device pointers. */
+GNC_API int gnc_fbp_correct(gnc_fbp_plan *plan, const float *d_proj, float *d_corrected,
+                            void *stream);
+/* Stage entry points used by tests and benchmarks. */
+GNC_API int gnc_fbp_stage(gnc_fbp_plan *plan, const float *d_input, void *stream);
+GNC_API int gnc_fbp_backproject(gnc_fbp_plan *plan, float *d_volume, int exact, void *stream);
+/* Backprojection of caller-provided staged rows (same layout as
+ * gnc_fbp_staged describes) with this plan's geometry. */
+GNC_API int gnc_fbp_backproject_staged(gnc_fbp_plan *plan, const void *d_staged,
+                                       const int8_t *d_row_exp, float *d_volume, int exact,
+                                       void *stream);
+/* int32 (T, Z, X) slab index the backprojector assigns (reconstructor.cpp:66-72). */
+GNC_API int gnc_fbp_slab_map(gnc_fbp_plan *plan, int32_t *d_out, void *stream);
+/* int8 (D, H, W/2 + 1) table of s(k) + s(-k) with s the phase-flip factor. */
+GNC_API int gnc_fbp_sign_table(gnc_fbp_plan *plan, int8_t *d_out, void *stream);
+/* Staged filtered rows: (ceil(H/2), D, T, W) pairs of float (F32) or half (F16),
+ * and for F16 the (ceil(H/2), D, T, 2) int8 row exponents (value = half * 2^-e). */
+GNC_API int gnc_fbp_staged(gnc_fbp_plan *plan, const void **d_staged, const int8_t **d_row_exp);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GUANACO_GB300_H */

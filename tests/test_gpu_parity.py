@@ -1,0 +1,286 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle and the
+golden vectors recorded from the reference.
+
+Tolerances (relative L2 over the whole output):
+  * FP32 path vs the reference CPU path (golden / float oracle): 1e-4
+  * FP16-staged path vs the FP64 oracle: 1e-3
+  * slab indices and phase-flip signs: bit-exact
+  * the exact backprojector given the oracle's filtered rows: bit-exact
+"""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import golden, golden_names
+
+pytestmark = pytest.mark.gpu
+
+FP32_TOL = 1e-4
+FP16_TOL = 1e-3
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA device")
+    from guanaco_gb300 import _lib
+
+    _lib.load()
+    return torch
+
+
+def dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+# --------------------------------------------------------- reference shapes
+def test_filter_matches_reference(torch):
+    from guanaco_gb300 import _lib
+
+    g = golden("filter")
+    L = _lib.load()
+    for k in g:
+        if not k.startswith("in_"):
+            continue
+        x = g[k]
+        d, t, n = x.shape
+        buf = dev(torch, x)
+        _lib.check(L.gnc_filter_device(n, t, d, buf.data_ptr(), None))
+        out = buf.cpu().numpy()
+        assert rel_l2(out, g["out_" + k[3:]]) < 1e-6
+
+
+@pytest.mark.parametrize("name", golden_names("recon_"))
+def test_recon_matches_reference(torch, name):
+    from guanaco_gb300 import detail
+
+    g = golden(name)
+    rec = np.zeros_like(g["rec"])
+    detail.recon(g["sino"], rec, g["angles"], float(g["centre"]), float(g["pixel_size"]),
+                 float(g["min_defocus"]), float(g["max_defocus"]), "gpu")
+    assert rel_l2(rec, g["rec"]) < FP32_TOL
+
+
+@pytest.mark.parametrize("name", golden_names("config_"))
+def test_config_grid_matches_reference(torch, name):
+    from guanaco_gb300 import detail
+
+    g = golden(name)
+    rec = np.zeros_like(g["rec"])
+    sino = g["sino"] if g["sino"].shape[0] > 1 else g["sino"][0]
+    detail.recon_grid(sino, rec, g["angles"], float(g["centre"]), float(g["pixel_size"]),
+                      float(g["min_defocus"]), float(g["max_defocus"]))
+    assert rel_l2(rec, g["rec"]) < FP32_TOL
+
+
+@pytest.mark.parametrize("name", golden_names("corr_"))
+def test_corr_matches_reference(torch, name):
+    from guanaco_gb300 import detail
+
+    g = golden(name)
+    rec = np.zeros_like(g["rec"])
+    ctf = g["ctf"] if g["ctf"].shape[0] > 1 else g["ctf"][0]
+    out = rec if g["ctf"].shape[0] > 1 else rec[0]
+    detail.corr(g["image"], ctf, out, "gpu")
+    assert rel_l2(rec, g["rec"]) < 1e-5
+
+
+@pytest.mark.parametrize("name", golden_names("pipeline_"))
+def test_pipeline_matches_reference(torch, name):
+    import guanaco_gb300 as G
+
+    g = golden(name)
+    proj, ang, centre = g["proj"], g["angles"], g["centre"]
+    df = None if math.isnan(float(g["defocus"])) else float(g["defocus"])
+    sdf = None if math.isnan(float(g["step_defocus"])) else float(g["step_defocus"])
+    ndf = int(g["num_defocus"]) or None
+    kw = dict(centre=centre, pixel_size=float(g["pixel_size"]), energy=float(g["energy"]),
+              defocus=df, num_defocus=ndf, step_defocus=sdf,
+              spherical_aberration=float(g["Cs"]), phase_shift=float(g["phase_shift"]))
+    # two calls, as the reference's reconstruct_file makes them
+    cp, mn, mx = G.correct_projections(proj, device="gpu", **{k: v for k, v in kw.items()})
+    if df is not None:
+        assert rel_l2(cp, g["corrected"].reshape(cp.shape)) < 1e-5
+        assert np.float32(mn) == np.float32(g["min_defocus"])
+    vol = G.reconstruct(cp, ang, None, centre, float(g["pixel_size"]), mn, mx,
+                        transform="minus" if bool(g["minus"]) else None,
+                        angular_weights=bool(g["angular_weights"]), device="gpu")
+    assert rel_l2(vol, g["volume"]) < FP32_TOL
+    # one fused device pass
+    vol2 = G.reconstruct_ctf(proj, ang, transform="minus" if bool(g["minus"]) else None,
+                             angular_weights=bool(g["angular_weights"]), **kw)
+    assert rel_l2(vol2, g["volume"]) < FP32_TOL
+
+
+# ------------------------------------------------------------ bit-exactness
+def _plan_case(oracle, T=17, H=12, W=48, Z=40, D=5, ps=1.0, Ca=0.0, phi=0.0, df=25000.0,
+               staging="f32", centre=None, weights=None, minus=False, seed=0, angles=None):
+    import guanaco_gb300 as G
+
+    rng = np.random.default_rng(seed)
+    ang = (np.deg2rad(np.linspace(-60, 60, T)) if angles is None else angles).astype(np.float32)
+    c = G.get_centre((T, H, W), centre, False)
+    mn, mx, step, nd = G.get_defocus_steps(df, D, None, W, c, ps)
+    slabs = G.api.slab_defoci(mn, nd, step)
+    plan = G.FbpPlan(T, H, W, ang, grid_height=Z, grid_width=W, centre=c, pixel_size=ps,
+                     input="raw", correct=True, num_defocus=nd, slab_defocus=slabs,
+                     min_defocus=float(mn - df), max_defocus=float(mx - df), energy=300,
+                     spherical_aberration=2.7, astigmatism=Ca, astigmatism_angle=30.0,
+                     phase_shift=phi, weights=weights, minus=minus, staging=staging)
+    ctf = oracle.ctf_stack(W, H, ps, 300, mn, nd, step, 2.7, Ca, 30.0, phi)
+    proj = rng.standard_normal((T, H, W)).astype(np.float32)
+    return plan, proj, ang, c, ctf, float(mn - df), float(mx - df)
+
+
+def _sym_sign(ctf):
+    s = -np.sign(ctf.imag.astype(np.float32)).astype(np.int32)
+    D, H, W = s.shape
+    m = s[:, (-np.arange(H)) % H][:, :, (-np.arange(W)) % W]
+    return (s + m)[:, :, : W // 2 + 1].astype(np.int8)
+
+
+@pytest.mark.parametrize("Ca,phi,ps", [(0.0, 0.0, 1.0), (0.0, 5.0, 1.35), (600.0, 2.0, 0.8)])
+def test_sign_table_bit_exact(torch, oracle, Ca, phi, ps):
+    plan, proj, *_ , ctf, mn, mx = _plan_case(oracle, H=36, W=40, D=4, ps=ps, Ca=Ca, phi=phi)
+    out = torch.empty((plan.D, plan.H, plan.W // 2 + 1), dtype=torch.int8, device="cuda")
+    plan.sign_table(out)
+    np.testing.assert_array_equal(out.cpu().numpy(), _sym_sign(ctf))
+
+
+@pytest.mark.parametrize("D,Z", [(5, 40), (10, 33), (3, 64)])
+def test_slab_map_bit_exact(torch, oracle, D, Z):
+    plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, D=D, Z=Z)
+    out = torch.empty((plan.T, Z, plan.W), dtype=torch.int32, device="cuda")
+    plan.slab_map(out)
+    ref = oracle.slab_index_map(plan.W, D, (Z, plan.W), ang, float(c[0]), 1.0, mn, mx)
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
+def _staged_from_rows(filtered_rows, H):
+    """Per-row filtered sinograms (H, D, T, N) -> staged pairs (H2, D, T, N, 2)."""
+    Hh, D, T, N = filtered_rows.shape
+    H2 = (H + 1) // 2
+    st = np.zeros((H2, D, T, N, 2), np.float32)
+    for y in range(H):
+        st[y // 2, :, :, :, y % 2] = filtered_rows[y]
+    return st
+
+
+def test_exact_backprojector_bit_exact(torch, oracle):
+    T, H, W, Z, D = 13, 5, 40, 36, 4
+    plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=T, H=H, W=W, Z=Z, D=D, seed=3)
+    rng = np.random.default_rng(7)
+    rows = rng.standard_normal((H, D, T, W)).astype(np.float32)
+    filt = np.stack([oracle.ramp_filter(rows[y], "f32") for y in range(H)])
+    staged = dev(torch, _staged_from_rows(filt, H))
+    vol = torch.empty((H, Z, W), dtype=torch.float32, device="cuda")
+    plan.backproject_staged(staged, None, vol, exact=True)
+    got = vol.cpu().numpy()
+    for y in range(H):
+        ref = oracle.project(filt[y], (Z, W), ang, float(c[y]), 1.0, mn, mx)
+        np.testing.assert_array_equal(got[y], ref)
+
+
+# ---------------------------------------------------------- whole pipeline
+def _oracle_volume(oracle, proj, ang, c, ctf, mn, mx, Z, precision, weights=None, minus=False):
+    return oracle.fbp_ctf(proj, ang, c, 1.0, ctf, mn, mx, weights, minus, Z=Z,
+                          precision=precision)
+
+
+@pytest.mark.parametrize("staging", ["f32", "f16"])
+@pytest.mark.parametrize("shape", [(17, 12, 48, 40, 5), (9, 7, 60, 30, 3), (21, 16, 64, 64, 1)])
+def test_pipeline_vs_oracles(torch, oracle, staging, shape):
+    T, H, W, Z, D = shape
+    plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=T, H=H, W=W, Z=Z, D=D, staging=staging)
+    vol = plan.execute_host(proj)
+    ref32 = _oracle_volume(oracle, proj, ang, c, ctf, mn, mx, Z, "f32")
+    ref64 = _oracle_volume(oracle, proj, ang, c, ctf, mn, mx, Z, "f64")
+    if staging == "f32":
+        assert rel_l2(vol, ref32) < FP32_TOL
+        assert rel_l2(vol, ref64) < FP32_TOL
+    else:
+        assert rel_l2(vol, ref64) < FP16_TOL
+
+
+def test_pipeline_exact_backprojector_equals_fast(torch, oracle):
+    plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=15, H=10, W=64, Z=48, D=6)
+    inp = dev(torch, proj)
+    a = torch.empty(plan.volume_shape, dtype=torch.float32, device="cuda")
+    b = torch.empty_like(a)
+    plan.stage(inp)
+    plan.backproject(a, exact=True)
+    plan.backproject(b, exact=False)
+    assert rel_l2(b.cpu().numpy(), a.cpu().numpy()) < 1e-5
+
+
+def test_weights_minus_and_offcentre_rows(torch, oracle):
+    T, H, W, Z = 11, 6, 40, 30
+    ang = np.deg2rad(np.linspace(-60, 60, T)).astype(np.float32)
+    import guanaco_gb300 as G
+
+    w = G.compute_angular_weights(ang)
+    centre = (W / 2 + np.linspace(-1.5, 2.0, H)).astype(np.float32)
+    plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=T, H=H, W=W, Z=Z, D=3, centre=centre,
+                                                 weights=w, minus=True)
+    vol = plan.execute_host(proj)
+    ref = _oracle_volume(oracle, proj, ang, c, ctf, mn, mx, Z, "f32", weights=w, minus=True)
+    assert rel_l2(vol, ref) < FP32_TOL
+
+
+@pytest.mark.parametrize("H", [1, 3, 8])
+def test_odd_and_tiny_heights(torch, oracle, H):
+    plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=7, H=H, W=32, Z=20, D=2)
+    vol = plan.execute_host(proj)
+    ref = _oracle_volume(oracle, proj, ang, c, ctf, mn, mx, 20, "f32")
+    assert rel_l2(vol, ref) < FP32_TOL
+
+
+def test_wide_tilt_range_and_single_tilt(torch, oracle):
+    ang = np.deg2rad(np.linspace(-90, 90, 9)).astype(np.float32)
+    plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=9, H=4, W=32, Z=32, D=4, angles=ang)
+    vol = plan.execute_host(proj)
+    ref = _oracle_volume(oracle, proj, ang, c, ctf, mn, mx, 32, "f32")
+    assert rel_l2(vol, ref) < FP32_TOL
+    one = np.array([0.2], np.float32)
+    plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=1, H=2, W=32, Z=16, D=1, angles=one)
+    vol = plan.execute_host(proj)
+    ref = _oracle_volume(oracle, proj, ang, c, ctf, mn, mx, 16, "f32")
+    assert rel_l2(vol, ref) < FP32_TOL
+
+
+def test_correct_only_matches_oracle(torch, oracle):
+    plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=5, H=30, W=40, D=3)
+    out = torch.empty((plan.T, plan.D, plan.H, plan.W), dtype=torch.float32, device="cuda")
+    plan.correct(dev(torch, proj), out)
+    got = out.cpu().numpy()
+    for t in range(plan.T):
+        assert rel_l2(got[t], oracle.correct(proj[t], ctf)) < 1e-5
+
+
+def test_linearity_at_full_detector_width(torch, oracle):
+    """Size-independent check at the 1024-px detector of the 3D-CTF config:
+    the path is linear in the projections."""
+    import guanaco_gb300 as G
+
+    T, H, W, Z, D = 9, 4, 1024, 64, 10
+    ang = np.deg2rad(np.linspace(-60, 60, T)).astype(np.float32)
+    c = G.get_centre((T, H, W), None, False)
+    mn, mx, step, nd = G.get_defocus_steps(30000.0, D, None, W, c, 1.0)
+    plan = G.FbpPlan(T, H, W, ang, grid_height=Z, centre=c, correct=True, num_defocus=nd,
+                     slab_defocus=G.api.slab_defoci(mn, nd, step), min_defocus=float(mn - 30000),
+                     max_defocus=float(mx - 30000), energy=300, spherical_aberration=2.7)
+    rng = np.random.default_rng(5)
+    a = rng.standard_normal((T, H, W)).astype(np.float32)
+    b = rng.standard_normal((T, H, W)).astype(np.float32)
+    va, vb = plan.execute_host(a), plan.execute_host(b)
+    vab = plan.execute_host((2.0 * a - 0.5 * b).astype(np.float32))
+    assert rel_l2(vab, 2.0 * va - 0.5 * vb) < 1e-5
