@@ -149,6 +149,7 @@ struct gnc_fbp_plan {
   TiltGeom *geom = nullptr;
   float *offset = nullptr;  // (H, T)
   float *tilt_factor = nullptr;
+  int *err = nullptr;        // device error word of the bounded waits
   size_t bytes = 0;
 };
 
@@ -162,6 +163,7 @@ static void plan_free(gnc_fbp_plan *p) {
   cudaFree(p->geom);
   cudaFree(p->offset);
   cudaFree(p->tilt_factor);
+  cudaFree(p->err);
 }
 
 template <typename T>
@@ -188,6 +190,7 @@ static BpArgs bp_args(const gnc_fbp_plan *p, float *vol) {
   a.doffset = p->doffset;
   a.uniform_centre = p->uniform_centre ? 1 : 0;
   a.vol = vol;
+  a.err = p->err;
   return a;
 }
 
@@ -278,12 +281,15 @@ int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
     p->sargs.phi = d->phase_shift_deg * M_PI / 180;
     p->sargs.slab_df = p->slab_df;
   }
-  const size_t elems = (size_t)p->Y2 * p->D * p->T * p->W;
+  // +8 pixels: a 16-byte aligned bulk copy of the last row may run past its end
+  const size_t elems = (size_t)p->Y2 * p->D * p->T * p->W + 8;
   if (e == cudaSuccess)
     e = p->staging == GNC_STAGE_F16 ? dalloc(p, (__half2 **)&p->staged, elems)
                                     : dalloc(p, (float2 **)&p->staged, elems);
   if (e == cudaSuccess && p->staging == GNC_STAGE_F16)
     e = dalloc(p, &p->row_exp, (size_t)p->Y2 * p->D * p->T * 2);
+  if (e == cudaSuccess) e = dalloc(p, &p->err, 1);
+  if (e == cudaSuccess) e = cudaMemset(p->err, 0, sizeof(int));
   if (e == cudaSuccess) e = dalloc(p, &p->geom, (size_t)p->T);
   if (e == cudaSuccess) e = dalloc(p, &p->offset, offset.size());
   if (e == cudaSuccess)
@@ -450,6 +456,20 @@ int gnc_fbp_slab_map(gnc_fbp_plan *p, int32_t *d_out, void *stream) {
   GNC_REQUIRE(p != nullptr && d_out != nullptr);
   BpArgs a = bp_args(p, nullptr);
   GNC_CUDA(launch_slab_map(a, d_out, (cudaStream_t)stream));
+  return GNC_OK;
+}
+
+int gnc_fbp_check(gnc_fbp_plan *p, void *stream) {
+  GNC_REQUIRE(p != nullptr);
+  int h = 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  GNC_CUDA(cudaMemcpyAsync(&h, p->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GNC_CUDA(cudaStreamSynchronize(s));
+  if (h != 0) {
+    GNC_CUDA(cudaMemsetAsync(p->err, 0, sizeof(int), s));
+    set_error("gnc_fbp_check: a device-side wait gave up (bulk copy never completed)");
+    return GNC_ERR_CUDA;
+  }
   return GNC_OK;
 }
 

@@ -133,9 +133,4 @@ cudaError_t launch_backproject_slice(const SliceBpArgs &a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-// The fast kernel is built in gnc_bp_fast.cu; until it is, use the exact one.
-cudaError_t launch_backproject_fast(const BpArgs &a, cudaStream_t s) {
-  return launch_backproject_exact(a, s);
-}
-
 }  // namespace gnc

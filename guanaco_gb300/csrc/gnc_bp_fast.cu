@@ -1,0 +1,446 @@
+// Fast backprojector: detector windows staged in shared memory by TMA bulk
+// copies, register accumulation of several voxels and Y rows per thread.
+//
+// Same arithmetic contract as the exact kernel (gnc_bp.cu) for everything that
+// decides *which* samples a voxel takes: the detector coordinate
+// ((x cos - z sin) + offset) - 0.5, its floor, the interpolation weight
+// t = pixel - floor and the edge rule 0 <= floor <= N-2 are the reference's
+// float operations (src/libguanaco/reconstructor.cpp:58-86), and the slab is
+// the reference's exact index.  The floor is taken without a float-to-int
+// conversion: adding 1.5 * 2^23 with round-toward-minus-infinity leaves
+// floor(pixel) in the low mantissa bits (|pixel| < 2^22).
+// Only the interpolation and the sum are reassociated:
+//   scale * ((1 - t) v0 + t v1)  ->  acc + scale * (v0 + t (v1 - v0)),
+// accumulated tilt by tilt in the reference's order.
+//
+// Tiling: a block owns a TX x TZ tile of (x, z) voxels for RP pairs of Y rows.
+// Lanes are 4 (x) by 8 (z); each thread holds A x B voxels (x stride 4, z
+// stride 8) for every row, so a warp's lanes read a compact run of detector
+// pixels.  Tilts are processed in groups of G.  For each tilt of a group the
+// block needs, per row pair and per slab its tile touches, the detector
+// pixels its tile projects onto; the lanes of warp 0 copy those row pieces
+// (float2 or half2 pixels: both rows of a pair) with cp.async.bulk into a
+// shared-memory buffer, tracked by an mbarrier.  Two buffers alternate, so
+// group g+1 is in flight while group g is accumulated.
+//
+// FP32 staging: v0, v1 are two 8-byte loads; FP16 staging: two 4-byte loads,
+// the interpolation is one half2 FMA and the sum one f32x2 FMA with
+// (scale 2^-e_a, scale 2^-e_b) for that row pair and slab.
+#include <cmath>
+
+#include "gnc_common.cuh"
+
+namespace gnc {
+
+namespace {
+
+constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+constexpr int kMagicBits = 0x4B400000;
+// bounded mbarrier wait: at most kWaitLimit polls of at most kWaitHintNs each
+constexpr unsigned kWaitLimit = 1u << 20;
+constexpr unsigned kWaitHintNs = 2000;
+
+__device__ __forceinline__ float voxel_coordf(int i, int n) {
+  return (float)((double)i - 0.5 * (double)n + 0.5);
+}
+
+// The reference's pixel coordinate (after the -0.5 shift), float, no FMA.
+__device__ __forceinline__ float detector_coord(float xc, float zs, float off) {
+  return __fsub_rn(__fadd_rn(__fsub_rn(xc, zs), off), 0.5f);
+}
+
+__device__ __forceinline__ int floor_int(float q) {
+  return __float_as_int(__fadd_rd(q, kMagic)) - kMagicBits;
+}
+
+typedef unsigned long long u64;
+
+// Two f32 lanes in one 64-bit register pair (sm_100 packed arithmetic).
+__device__ __forceinline__ u64 f2_pack(float lo, float hi) {
+  u64 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ float2 f2_unpack(u64 v) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+__device__ __forceinline__ u64 f2_sub(u64 a, u64 b) {
+  u64 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ u64 f2_fma(u64 a, u64 b, u64 c) {  // a * b + c
+  u64 r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+
+// ---- mbarrier / bulk copy (PTX) ------------------------------------------
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(u64 *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(u64 *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, u64 *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+// Waits for the phase with the given parity; gives up after kWaitLimit polls
+// and reports it through *err instead of spinning forever.
+__device__ __forceinline__ void mbar_wait(u64 *bar, unsigned parity, int *err) {
+  for (unsigned it = 0; it < kWaitLimit; ++it) {
+    unsigned done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3; "
+        "selp.u32 %0, 1, 0, p; }"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(kWaitHintNs)
+        : "memory");
+    if (done) return;
+  }
+  if (err) atomicOr(err, 1);
+}
+
+// ceil(sqrt(v)) for a non-negative integer, at compile time
+constexpr int isqrt_ceil(int v) {
+  int r = 0;
+  while (r * r < v) ++r;
+  return r;
+}
+
+struct TiltParams {
+  float cos_a, sin_a, off;
+  int p_s;      // first staged pixel (aligned down for the bulk copy)
+  int k0, nk;   // first slab and slab count of the tile
+  int edge;     // the tile's window reaches outside [0, N-2]
+  int pad;
+};
+
+}  // namespace
+
+template <int RP, int KMAX, int G, bool F16>
+struct FastBp {
+  static constexpr int A = 2, B = 4;              // voxels per thread in x and z
+  static constexpr int WX = 4, WZ = 2;            // warps per block in x and z
+  static constexpr int TX = 4 * A * WX;           // tile width (x)
+  static constexpr int TZ = 8 * B * WZ;           // tile height (z)
+  static constexpr int NT = 32 * WX * WZ;         // threads
+  static constexpr int PB = F16 ? 4 : 8;          // bytes per staged pixel (both rows)
+  static constexpr int ALIGN = 16 / PB;           // pixels per 16 bytes
+  // widest detector window of a TX x TZ tile: (TX-1)|c| + (TZ-1)|s| <=
+  // sqrt(TX^2 + TZ^2); plus the right neighbour, alignment and slack
+  static constexpr int SLOT = ((isqrt_ceil(TX * TX + TZ * TZ) + 4 + 2 * ALIGN) / ALIGN) * ALIGN;
+  static constexpr int SLOT_BYTES = SLOT * PB;
+  static constexpr int ROWS = G * RP * KMAX;      // slots per buffer
+  static constexpr size_t BUF = (size_t)ROWS * SLOT_BYTES;
+  static constexpr size_t SMEM = 2 * BUF + 16;    // two buffers + a zero pixel pair
+};
+
+template <int RP, int KMAX, int G, bool F16>
+__global__ void __launch_bounds__(256, 2)
+k_bp_fast(BpArgs a) {
+  using P = FastBp<RP, KMAX, G, F16>;
+  constexpr int A = P::A, B = P::B;
+  constexpr int TCH = 128;  // tilts whose parameters are held at once
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ TiltParams s_tp[TCH];
+  __shared__ float2 s_rs[TCH * RP * KMAX];  // per (tilt, row pair, slab) scale
+  __shared__ __align__(8) u64 s_bar[2];
+
+  const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int lx = lane >> 3, lz = lane & 7;
+  const int wx = warp % P::WX, wz = warp / P::WX;
+  const int x0 = blockIdx.x * P::TX, z0 = blockIdx.y * P::TZ;
+  const int y2_0 = blockIdx.z * RP;
+  const int Y2 = (a.Y + 1) / 2;
+  unsigned char *zero_pair = smem_raw + 2 * P::BUF;  // 16 zero bytes
+
+  float xf[A], zf[B];
+#pragma unroll
+  for (int i = 0; i < A; ++i) xf[i] = voxel_coordf(x0 + wx * 4 * A + 4 * i + lx, a.X);
+#pragma unroll
+  for (int j = 0; j < B; ++j) zf[j] = voxel_coordf(z0 + wz * 8 * B + 8 * j + lz, a.Z);
+  const float cx0 = voxel_coordf(x0, a.X), cx1 = voxel_coordf(x0 + P::TX - 1, a.X);
+  const float cz0 = voxel_coordf(z0, a.Z), cz1 = voxel_coordf(z0 + P::TZ - 1, a.Z);
+
+  if (tid == 0) {
+    // every lane of warp 0 arrives once per phase (with its own byte count)
+    mbar_init(&s_bar[0], 32);
+    mbar_init(&s_bar[1], 32);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (tid < 4) ((unsigned *)zero_pair)[tid] = 0u;
+
+  // Bulk copies of the window rows of chunk tilts [tg, tg + ng) into buffer b,
+  // issued by the 32 lanes of warp 0 (each arrives on the barrier once).
+  auto issue_copies = [&](int tg_local, int ng, int tbase, int b) {
+    unsigned char *buf = smem_raw + b * P::BUF;
+    int nslot[(P::ROWS + 31) / 32];
+    unsigned bytes = 0;
+#pragma unroll
+    for (int q = 0; q < (P::ROWS + 31) / 32; ++q) {
+      const int slot = lane + 32 * q;
+      nslot[q] = 0;
+      if (slot < P::ROWS) {
+        const int gi = slot / (RP * KMAX), r = (slot / KMAX) % RP, sl = slot % KMAX;
+        if (gi < ng && y2_0 + r < Y2) {
+          const TiltParams tp = s_tp[tg_local + gi];
+          const int n_px = ((tp.pad - tp.p_s + 1 + P::ALIGN - 1) / P::ALIGN) * P::ALIGN;
+          if (sl < tp.nk && n_px > 0) {
+            nslot[q] = n_px;
+            bytes += n_px * P::PB;
+          }
+        }
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(&s_bar[b], bytes);
+#pragma unroll
+    for (int q = 0; q < (P::ROWS + 31) / 32; ++q) {
+      if (nslot[q] > 0) {
+        const int slot = lane + 32 * q;
+        const int gi = slot / (RP * KMAX), r = (slot / KMAX) % RP, sl = slot % KMAX;
+        const TiltParams tp = s_tp[tg_local + gi];
+        const size_t row = ((size_t)(y2_0 + r) * a.D + (tp.k0 + sl)) * a.T + (tbase + tg_local + gi);
+        const unsigned char *src = (const unsigned char *)a.staged + (row * a.N + tp.p_s) * P::PB;
+        bulk_g2s(buf + slot * P::SLOT_BYTES, src, nslot[q] * P::PB, &s_bar[b]);
+      }
+    }
+  };
+
+  u64 acc[A][B][RP];
+#pragma unroll
+  for (int i = 0; i < A; ++i)
+#pragma unroll
+    for (int j = 0; j < B; ++j)
+#pragma unroll
+      for (int r = 0; r < RP; ++r) acc[i][j][r] = 0ull;
+
+  int gg = 0;  // groups started so far: buffer gg & 1, use (gg >> 1) of it
+  for (int tbase = 0; tbase < a.T; tbase += TCH) {
+    const int nch = min(TCH, a.T - tbase);
+    __syncthreads();  // the previous chunk's parameters and buffers are no longer read
+    for (int tl = tid; tl < nch; tl += P::NT) {
+      const int t = tbase + tl;
+      const TiltGeom g = a.geom[t];
+      const float offt = a.offset[t];
+      // the exact coordinate is monotone in x and in z: extremes at corners
+      const float xc0 = __fmul_rn(cx0, g.cos_a), xc1 = __fmul_rn(cx1, g.cos_a);
+      const float zs0 = __fmul_rn(cz0, g.sin_a), zs1 = __fmul_rn(cz1, g.sin_a);
+      const float q00 = detector_coord(xc0, zs0, offt), q01 = detector_coord(xc0, zs1, offt);
+      const float q10 = detector_coord(xc1, zs0, offt), q11 = detector_coord(xc1, zs1, offt);
+      const int p_lo = floor_int(fminf(fminf(q00, q01), fminf(q10, q11)));
+      const int p_hi = floor_int(fmaxf(fmaxf(q00, q01), fmaxf(q10, q11)));
+      int k_lo = 0, k_hi = 0;
+      if (a.D > 1) {
+        const int k00 = slab_index(cx0, cz0, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
+        const int k01 = slab_index(cx0, cz1, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
+        const int k10 = slab_index(cx1, cz0, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
+        const int k11 = slab_index(cx1, cz1, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
+        k_lo = min(min(k00, k01), min(k10, k11));
+        k_hi = max(max(k00, k01), max(k10, k11));
+      }
+      TiltParams tp;
+      tp.cos_a = g.cos_a;
+      tp.sin_a = g.sin_a;
+      tp.off = offt;
+      tp.p_s = (max(p_lo, 0) / P::ALIGN) * P::ALIGN;
+      tp.k0 = k_lo;
+      tp.nk = min(k_hi - k_lo + 1, KMAX);
+      tp.edge = (p_lo < 0 || p_hi > a.N - 2) ? 1 : 0;
+      tp.pad = min(p_hi + 1, a.N - 1);  // last pixel a voxel of the tile can read
+      s_tp[tl] = tp;
+    }
+    // scale per (tilt, row pair, slab): the BP scale, times 2^-e of each row (F16)
+    for (int e = tid; e < nch * RP * KMAX; e += P::NT) {
+      const float sc = a.geom[tbase + e / (RP * KMAX)].scale;
+      s_rs[e] = make_float2(sc, sc);
+    }
+    __syncthreads();
+    if (F16) {
+      for (int e = tid; e < nch * RP * KMAX; e += P::NT) {
+        const int tl = e / (RP * KMAX), r = (e / KMAX) % RP, sl = e % KMAX;
+        const int y2 = y2_0 + r;
+        const TiltParams tp = s_tp[tl];
+        if (y2 < Y2 && sl < tp.nk) {
+          const size_t row = ((size_t)y2 * a.D + (tp.k0 + sl)) * a.T + (tbase + tl);
+          const float2 f = s_rs[e];
+          s_rs[e] = make_float2(f.x * __int_as_float((127 - a.row_exp[2 * row]) << 23),
+                                f.y * __int_as_float((127 - a.row_exp[2 * row + 1]) << 23));
+        }
+      }
+      __syncthreads();
+    }
+    const int ngroups = (nch + G - 1) / G;
+    if (warp == 0) issue_copies(0, min(G, nch), tbase, gg & 1);
+    for (int grp = 0; grp < ngroups; ++grp, ++gg) {
+      const int b = gg & 1;
+      const int tg = grp * G;  // within the chunk
+      const int ng = min(G, nch - tg);
+      __syncthreads();  // everyone is done with buffer b^1
+      if (warp == 0 && grp + 1 < ngroups)
+        issue_copies(tg + G, min(G, nch - tg - G), tbase, b ^ 1);
+      mbar_wait(&s_bar[b], (gg >> 1) & 1, a.err);
+      const unsigned char *buf = smem_raw + b * P::BUF;
+      for (int gi = 0; gi < ng; ++gi) {
+        const TiltParams tp = s_tp[tg + gi];
+        float xc[A], zs[B];
+#pragma unroll
+        for (int i = 0; i < A; ++i) xc[i] = __fmul_rn(xf[i], tp.cos_a);
+#pragma unroll
+        for (int j = 0; j < B; ++j) zs[j] = __fmul_rn(zf[j], tp.sin_a);
+        // slab of this thread's voxels: the tile's when it has one; otherwise
+        // the extremes over the thread's box (height is monotone in x and z)
+        int kl = tp.k0, kh = tp.k0;
+        if (tp.nk > 1) {
+          const bool xs = tp.sin_a > 0.f, zc = tp.cos_a > 0.f;
+          const int ka = slab_index(xs ? xf[A - 1] : xf[0], zc ? zf[B - 1] : zf[0], tp.sin_a,
+                                    tp.cos_a, a.dscale, a.doffset, a.D);
+          const int kb = slab_index(xs ? xf[0] : xf[A - 1], zc ? zf[0] : zf[B - 1], tp.sin_a,
+                                    tp.cos_a, a.dscale, a.doffset, a.D);
+          kl = min(ka, kb);
+          kh = max(ka, kb);
+        }
+        const bool uniform = kl == kh;
+        const unsigned char *tbuf = buf + (size_t)gi * RP * KMAX * P::SLOT_BYTES;
+        const float2 *trs = s_rs + (size_t)(tg + gi) * RP * KMAX;
+        // byte offset of pixel p of slot (r, s): ((r * KMAX + s) * SLOT + p - p_s) * PB;
+        // the magic-number bias of the float bits folds into the same constant
+        const unsigned base_u =
+            (unsigned)(((kl - tp.k0) * P::SLOT - tp.p_s) * P::PB) - (unsigned)kMagicBits * P::PB;
+        u64 rs[RP];
+#pragma unroll
+        for (int rr = 0; rr < RP; ++rr) {
+          const float2 f = trs[rr * KMAX + (kl - tp.k0)];
+          rs[rr] = f2_pack(f.x, f.y);
+        }
+#pragma unroll
+        for (int i = 0; i < A; ++i) {
+#pragma unroll
+          for (int j = 0; j < B; ++j) {
+            const float q = detector_coord(xc[i], zs[j], tp.off);
+            const float r = __fadd_rd(q, kMagic);
+            const float t = __fsub_rn(q, __fsub_rn(r, kMagic));
+            int ks = kl - tp.k0;
+            unsigned off = base_u;
+            if (!uniform) {
+              ks = slab_index(xf[i], zf[j], tp.sin_a, tp.cos_a, a.dscale, a.doffset, a.D) - tp.k0;
+              off = (unsigned)((ks * P::SLOT - tp.p_s) * P::PB) - (unsigned)kMagicBits * P::PB;
+            }
+            // unsigned arithmetic wraps modulo 2^32: the bias cancels exactly
+            off += (unsigned)__float_as_int(r) * (unsigned)P::PB;
+            const unsigned char *p0 = tbuf + off;
+            bool valid = true;
+            if (tp.edge) {
+              const unsigned ind = (unsigned)(__float_as_int(r) - kMagicBits);
+              valid = ind <= (unsigned)(a.N - 2);
+            }
+            if (F16) {
+              const __half2 t2 = __float2half2_rn(t);
+#pragma unroll
+              for (int rr = 0; rr < RP; ++rr) {
+                const unsigned char *p = valid ? p0 + rr * KMAX * P::SLOT_BYTES : zero_pair;
+                const __half2 v0 = *(const __half2 *)p, v1 = *(const __half2 *)(p + 4);
+                const float2 val = __half22float2(__hfma2(t2, __hsub2(v1, v0), v0));
+                u64 sc = rs[rr];
+                if (!uniform) {
+                  const float2 f = trs[rr * KMAX + ks];
+                  sc = f2_pack(f.x, f.y);
+                }
+                acc[i][j][rr] = f2_fma(f2_pack(val.x, val.y), sc, acc[i][j][rr]);
+              }
+            } else {
+              const u64 tt = f2_pack(t, t);
+#pragma unroll
+              for (int rr = 0; rr < RP; ++rr) {
+                const unsigned char *p = valid ? p0 + rr * KMAX * P::SLOT_BYTES : zero_pair;
+                const u64 v0 = *(const u64 *)p, v1 = *(const u64 *)(p + 8);
+                const u64 val = f2_fma(tt, f2_sub(v1, v0), v0);
+                u64 sc = rs[rr];
+                if (!uniform) {
+                  const float2 f = trs[rr * KMAX + ks];
+                  sc = f2_pack(f.x, f.y);
+                }
+                acc[i][j][rr] = f2_fma(val, sc, acc[i][j][rr]);
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  // ---- store
+#pragma unroll
+  for (int rr = 0; rr < RP; ++rr) {
+    const int ya = 2 * (y2_0 + rr), yb = ya + 1;
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      const int z = z0 + wz * 8 * B + 8 * j + lz;
+      if (z >= a.Z) continue;
+#pragma unroll
+      for (int i = 0; i < A; ++i) {
+        const int x = x0 + wx * 4 * A + 4 * i + lx;
+        if (x >= a.X) continue;
+        const float2 v = f2_unpack(acc[i][j][rr]);
+        if (ya < a.Y) a.vol[((size_t)ya * a.Z + z) * a.X + x] = v.x;
+        if (yb < a.Y) a.vol[((size_t)yb * a.Z + z) * a.X + x] = v.y;
+      }
+    }
+  }
+}
+
+template <int RP, int KMAX, int G, bool F16>
+static cudaError_t launch_fast(const BpArgs &a, cudaStream_t s) {
+  using P = FastBp<RP, KMAX, G, F16>;
+  auto kern = k_bp_fast<RP, KMAX, G, F16>;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM);
+    attr = true;
+  }
+  const int Y2 = (a.Y + 1) / 2;
+  dim3 grid((a.X + P::TX - 1) / P::TX, (a.Z + P::TZ - 1) / P::TZ, (Y2 + RP - 1) / RP);
+  kern<<<grid, P::NT, P::SMEM, s>>>(a);
+  return cudaGetLastError();
+}
+
+// Slabs a TX x TZ tile can touch for one tilt: its height span is at most
+// sqrt(TX^2 + TZ^2) pixels and a slab is 1 / dscale pixels thick.
+static int max_slabs_per_tile(const BpArgs &a, int TX, int TZ) {
+  if (a.D <= 1) return 1;
+  double span = std::sqrt((double)TX * TX + (double)TZ * TZ) + 2.0;
+  return (int)std::ceil(span * std::fabs((double)a.dscale)) + 1;
+}
+
+bool backproject_fast_supported(const BpArgs &a) {
+  using P = FastBp<4, 2, 8, false>;
+  // 16-byte aligned staged rows for the bulk copies; the fast path covers up to
+  // four slabs per tile and a shared centre
+  const int align_px = a.staging == kStageF16 ? 4 : 2;
+  return a.uniform_centre && a.N % align_px == 0 && max_slabs_per_tile(a, P::TX, P::TZ) <= 4 &&
+         a.N >= 2;
+}
+
+cudaError_t launch_backproject_fast(const BpArgs &a, cudaStream_t s) {
+  using P = FastBp<4, 2, 8, false>;
+  if (!backproject_fast_supported(a)) return launch_backproject_exact(a, s);
+  const int need = max_slabs_per_tile(a, P::TX, P::TZ);
+  const bool f16 = a.staging == kStageF16;
+  if (need <= 2)
+    return f16 ? launch_fast<4, 2, 8, true>(a, s) : launch_fast<4, 2, 8, false>(a, s);
+  return f16 ? launch_fast<4, 4, 4, true>(a, s) : launch_fast<4, 4, 4, false>(a, s);
+}
+
+}  // namespace gnc

@@ -101,7 +101,11 @@ struct BpArgs {
   float dscale, doffset;  // slab map (reconstructor.cpp:28-32)
   int uniform_centre;     // all rows share one centre
   float *vol;             // (Y, Z, X)
+  int *err;               // device error word (bounded waits that gave up), or null
 };
+// The fast kernel's requirements (shared centre, 16-byte aligned rows, at most
+// four slabs per tile); launch_backproject_fast falls back to the exact kernel.
+bool backproject_fast_supported(const BpArgs &a);
 cudaError_t launch_backproject_exact(const BpArgs &a, cudaStream_t s);
 cudaError_t launch_backproject_fast(const BpArgs &a, cudaStream_t s);
 cudaError_t launch_slab_map(const BpArgs &a, int32_t *out, cudaStream_t s);

@@ -157,6 +157,10 @@ class FbpPlan:
     def sign_table(self, out, stream=None):
         _lib.check(self._lib.gnc_fbp_sign_table(self._h, _ptr(out), _stream(stream)))
 
+    def check(self, stream=None):
+        """Synchronise and raise if a bounded device-side wait gave up."""
+        _lib.check(self._lib.gnc_fbp_check(self._h, _stream(stream)))
+
     def staged(self):
         """(device pointer of the staged rows, device pointer of the F16 exponents)."""
         s = ctypes.c_void_p()

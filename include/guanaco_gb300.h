@@ -199,6 +199,10 @@ GNC_API int gnc_fbp_backproject_staged(gnc_fbp_plan *plan, const void *d_staged,
 GNC_API int gnc_fbp_slab_map(gnc_fbp_plan *plan, int32_t *d_out, void *stream);
 /* int8 (D, H, W/2 + 1) table of s(k) + s(-k) with s the phase-flip factor. */
 GNC_API int gnc_fbp_sign_table(gnc_fbp_plan *plan, int8_t *d_out, void *stream);
+/* Synchronises `stream` and reports (then clears) a device-side error of the
+ * plan's kernels: every wait in them is bounded and records a timeout here
+ * instead of hanging. */
+GNC_API int gnc_fbp_check(gnc_fbp_plan *plan, void *stream);
 /* Staged filtered rows: (ceil(H/2), D, T, W) pairs of float (F32) or half (F16),
  * and for F16 the (ceil(H/2), D, T, 2) int8 row exponents (value = half * 2^-e). */
 GNC_API int gnc_fbp_staged(gnc_fbp_plan *plan, const void **d_staged, const int8_t **d_row_exp);
