@@ -120,11 +120,11 @@ constexpr int isqrt_ceil(int v) {
 }
 
 struct TiltParams {
-  float cos_a, sin_a, off;
+  float cos_a, sin_a, off, scale;
   int p_s;      // first staged pixel (aligned down for the bulk copy)
   int k0, nk;   // first slab and slab count of the tile
   int edge;     // the tile's window reaches outside [0, N-2]
-  int pad;
+  int pad;      // last pixel a voxel of the tile can read
 };
 
 }  // namespace
@@ -139,12 +139,17 @@ struct FastBp {
   static constexpr int PB = F16 ? 4 : 8;          // bytes per staged pixel (both rows)
   static constexpr int ALIGN = 16 / PB;           // pixels per 16 bytes
   // widest detector window of a TX x TZ tile: (TX-1)|c| + (TZ-1)|s| <=
-  // sqrt(TX^2 + TZ^2); plus the right neighbour, alignment and slack
-  static constexpr int SLOT = ((isqrt_ceil(TX * TX + TZ * TZ) + 4 + 2 * ALIGN) / ALIGN) * ALIGN;
+  // sqrt(TX^2 + TZ^2); plus the right neighbour and slack
+  static constexpr int WIN = isqrt_ceil(TX * TX + TZ * TZ) + 4;
+  // pixels a bulk copy may write into one slot (window + alignment, rounded)
+  static constexpr int NPX_MAX = ((WIN + 2 * ALIGN) / ALIGN) * ALIGN;
+  // every slot ends in ALIGN zero pixels that copies never touch: voxels off
+  // the detector read their (v0, v1) pair there
+  static constexpr int SLOT = NPX_MAX + ALIGN;
   static constexpr int SLOT_BYTES = SLOT * PB;
   static constexpr int ROWS = G * RP * KMAX;      // slots per buffer
   static constexpr size_t BUF = (size_t)ROWS * SLOT_BYTES;
-  static constexpr size_t SMEM = 2 * BUF + 16;    // two buffers + a zero pixel pair
+  static constexpr size_t SMEM = 2 * BUF;         // two buffers
 };
 
 template <int RP, int KMAX, int G, bool F16>
@@ -165,7 +170,6 @@ k_bp_fast(BpArgs a) {
   const int x0 = blockIdx.x * P::TX, z0 = blockIdx.y * P::TZ;
   const int y2_0 = blockIdx.z * RP;
   const int Y2 = (a.Y + 1) / 2;
-  unsigned char *zero_pair = smem_raw + 2 * P::BUF;  // 16 zero bytes
 
   float xf[A], zf[B];
 #pragma unroll
@@ -181,7 +185,8 @@ k_bp_fast(BpArgs a) {
     mbar_init(&s_bar[1], 32);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (tid < 4) ((unsigned *)zero_pair)[tid] = 0u;
+  for (int z = tid; z < 2 * P::ROWS; z += P::NT)  // the zero pixels of every slot
+    *(uint4 *)(smem_raw + (size_t)z * P::SLOT_BYTES + P::NPX_MAX * P::PB) = make_uint4(0, 0, 0, 0);
 
   // Bulk copies of the window rows of chunk tilts [tg, tg + ng) into buffer b,
   // issued by the 32 lanes of warp 0 (each arrives on the barrier once).
@@ -197,7 +202,8 @@ k_bp_fast(BpArgs a) {
         const int gi = slot / (RP * KMAX), r = (slot / KMAX) % RP, sl = slot % KMAX;
         if (gi < ng && y2_0 + r < Y2) {
           const TiltParams tp = s_tp[tg_local + gi];
-          const int n_px = ((tp.pad - tp.p_s + 1 + P::ALIGN - 1) / P::ALIGN) * P::ALIGN;
+          const int n_px =
+              min(((tp.pad - tp.p_s + 1 + P::ALIGN - 1) / P::ALIGN) * P::ALIGN, P::NPX_MAX);
           if (sl < tp.nk && n_px > 0) {
             nslot[q] = n_px;
             bytes += n_px * P::PB;
@@ -256,11 +262,12 @@ k_bp_fast(BpArgs a) {
       tp.cos_a = g.cos_a;
       tp.sin_a = g.sin_a;
       tp.off = offt;
+      tp.scale = g.scale;
       tp.p_s = (max(p_lo, 0) / P::ALIGN) * P::ALIGN;
       tp.k0 = k_lo;
       tp.nk = min(k_hi - k_lo + 1, KMAX);
       tp.edge = (p_lo < 0 || p_hi > a.N - 2) ? 1 : 0;
-      tp.pad = min(p_hi + 1, a.N - 1);  // last pixel a voxel of the tile can read
+      tp.pad = min(p_hi + 1, a.N - 1);
       s_tp[tl] = tp;
     }
     // scale per (tilt, row pair, slab): the BP scale, times 2^-e of each row (F16)
@@ -301,30 +308,53 @@ k_bp_fast(BpArgs a) {
         for (int i = 0; i < A; ++i) xc[i] = __fmul_rn(xf[i], tp.cos_a);
 #pragma unroll
         for (int j = 0; j < B; ++j) zs[j] = __fmul_rn(zf[j], tp.sin_a);
-        // slab of this thread's voxels: the tile's when it has one; otherwise
-        // the extremes over the thread's box (height is monotone in x and z)
-        int kl = tp.k0, kh = tp.k0;
+        // Slab of each voxel.  Within the tile k = k0 + #{m in [1, nk) :
+        // defocus >= k0 + m - 1/2}: the reference's clamp(floor(defocus + 1/2))
+        // with the floor replaced by exact comparisons.  The defocus is the
+        // reference's float expression, monotone in x and z, so the thread's
+        // extremes sit at two opposite corners of its voxel box.
+        float xs[A], zc[B];
+        int cl = 0;
+        bool uniform = true;
         if (tp.nk > 1) {
-          const bool xs = tp.sin_a > 0.f, zc = tp.cos_a > 0.f;
-          const int ka = slab_index(xs ? xf[A - 1] : xf[0], zc ? zf[B - 1] : zf[0], tp.sin_a,
-                                    tp.cos_a, a.dscale, a.doffset, a.D);
-          const int kb = slab_index(xs ? xf[0] : xf[A - 1], zc ? zf[0] : zf[B - 1], tp.sin_a,
-                                    tp.cos_a, a.dscale, a.doffset, a.D);
-          kl = min(ka, kb);
-          kh = max(ka, kb);
+#pragma unroll
+          for (int i = 0; i < A; ++i) xs[i] = __fmul_rn(-xf[i], tp.sin_a);
+#pragma unroll
+          for (int j = 0; j < B; ++j) zc[j] = __fmul_rn(zf[j], tp.cos_a);
+          const float xsl = tp.sin_a > 0.f ? xs[A - 1] : xs[0];
+          const float xsh = tp.sin_a > 0.f ? xs[0] : xs[A - 1];
+          const float zcl = tp.cos_a > 0.f ? zc[B - 1] : zc[0];
+          const float zch = tp.cos_a > 0.f ? zc[0] : zc[B - 1];
+          const float dl = __fadd_rn(__fmul_rn(__fsub_rn(xsl, zcl), a.dscale), a.doffset);
+          const float dh = __fadd_rn(__fmul_rn(__fsub_rn(xsh, zch), a.dscale), a.doffset);
+          int ch = 0;
+#pragma unroll
+          for (int m = 1; m < KMAX; ++m) {
+            const float bnd = (float)(tp.k0 + m) - 0.5f;
+            cl += (m < tp.nk && dl >= bnd) ? 1 : 0;
+            ch += (m < tp.nk && dh >= bnd) ? 1 : 0;
+          }
+          const int lo = min(cl, ch);
+          uniform = lo == max(cl, ch);
+          cl = lo;
         }
-        const bool uniform = kl == kh;
         const unsigned char *tbuf = buf + (size_t)gi * RP * KMAX * P::SLOT_BYTES;
         const float2 *trs = s_rs + (size_t)(tg + gi) * RP * KMAX;
-        // byte offset of pixel p of slot (r, s): ((r * KMAX + s) * SLOT + p - p_s) * PB;
-        // the magic-number bias of the float bits folds into the same constant
-        const unsigned base_u =
-            (unsigned)(((kl - tp.k0) * P::SLOT - tp.p_s) * P::PB) - (unsigned)kMagicBits * P::PB;
+        // byte offset of pixel p of slot (r, s): (r * KMAX + s) * SLOT_BYTES + (p - p_s) * PB;
+        // the magic-number bias of the float bits folds into the same
+        // constant (unsigned arithmetic wraps modulo 2^32 and cancels exactly)
+        const unsigned bias = (unsigned)(-tp.p_s * P::PB) - (unsigned)kMagicBits * P::PB;
+        const unsigned base_u = (unsigned)(cl * P::SLOT_BYTES) + bias;
         u64 rs[RP];
+        if (F16) {
 #pragma unroll
-        for (int rr = 0; rr < RP; ++rr) {
-          const float2 f = trs[rr * KMAX + (kl - tp.k0)];
-          rs[rr] = f2_pack(f.x, f.y);
+          for (int rr = 0; rr < RP; ++rr) {
+            const float2 f = trs[rr * KMAX + cl];
+            rs[rr] = f2_pack(f.x, f.y);
+          }
+        } else {
+#pragma unroll
+          for (int rr = 0; rr < RP; ++rr) rs[rr] = f2_pack(tp.scale, tp.scale);
         }
 #pragma unroll
         for (int i = 0; i < A; ++i) {
@@ -333,30 +363,33 @@ k_bp_fast(BpArgs a) {
             const float q = detector_coord(xc[i], zs[j], tp.off);
             const float r = __fadd_rd(q, kMagic);
             const float t = __fsub_rn(q, __fsub_rn(r, kMagic));
-            int ks = kl - tp.k0;
             unsigned off = base_u;
+            int c = cl;
             if (!uniform) {
-              ks = slab_index(xf[i], zf[j], tp.sin_a, tp.cos_a, a.dscale, a.doffset, a.D) - tp.k0;
-              off = (unsigned)((ks * P::SLOT - tp.p_s) * P::PB) - (unsigned)kMagicBits * P::PB;
+              const float d = __fadd_rn(__fmul_rn(__fsub_rn(xs[i], zc[j]), a.dscale), a.doffset);
+              c = 0;
+#pragma unroll
+              for (int m = 1; m < KMAX; ++m)
+                c += (m < tp.nk && d >= (float)(tp.k0 + m) - 0.5f) ? 1 : 0;
+              off = (unsigned)(c * P::SLOT_BYTES) + bias;
             }
-            // unsigned arithmetic wraps modulo 2^32: the bias cancels exactly
             off += (unsigned)__float_as_int(r) * (unsigned)P::PB;
-            const unsigned char *p0 = tbuf + off;
-            bool valid = true;
             if (tp.edge) {
+              // the reference skips samples unless 0 <= floor <= N-2
               const unsigned ind = (unsigned)(__float_as_int(r) - kMagicBits);
-              valid = ind <= (unsigned)(a.N - 2);
+              if (ind > (unsigned)(a.N - 2)) off = P::NPX_MAX * P::PB;
             }
+            const unsigned char *p0 = tbuf + off;
             if (F16) {
               const __half2 t2 = __float2half2_rn(t);
 #pragma unroll
               for (int rr = 0; rr < RP; ++rr) {
-                const unsigned char *p = valid ? p0 + rr * KMAX * P::SLOT_BYTES : zero_pair;
+                const unsigned char *p = p0 + rr * KMAX * P::SLOT_BYTES;
                 const __half2 v0 = *(const __half2 *)p, v1 = *(const __half2 *)(p + 4);
                 const float2 val = __half22float2(__hfma2(t2, __hsub2(v1, v0), v0));
                 u64 sc = rs[rr];
                 if (!uniform) {
-                  const float2 f = trs[rr * KMAX + ks];
+                  const float2 f = trs[rr * KMAX + c];
                   sc = f2_pack(f.x, f.y);
                 }
                 acc[i][j][rr] = f2_fma(f2_pack(val.x, val.y), sc, acc[i][j][rr]);
@@ -365,15 +398,10 @@ k_bp_fast(BpArgs a) {
               const u64 tt = f2_pack(t, t);
 #pragma unroll
               for (int rr = 0; rr < RP; ++rr) {
-                const unsigned char *p = valid ? p0 + rr * KMAX * P::SLOT_BYTES : zero_pair;
+                const unsigned char *p = p0 + rr * KMAX * P::SLOT_BYTES;
                 const u64 v0 = *(const u64 *)p, v1 = *(const u64 *)(p + 8);
                 const u64 val = f2_fma(tt, f2_sub(v1, v0), v0);
-                u64 sc = rs[rr];
-                if (!uniform) {
-                  const float2 f = trs[rr * KMAX + ks];
-                  sc = f2_pack(f.x, f.y);
-                }
-                acc[i][j][rr] = f2_fma(val, sc, acc[i][j][rr]);
+                acc[i][j][rr] = f2_fma(val, rs[rr], acc[i][j][rr]);
               }
             }
           }

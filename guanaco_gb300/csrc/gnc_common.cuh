@@ -122,6 +122,16 @@ struct SliceBpArgs {
 };
 cudaError_t launch_backproject_slice(const SliceBpArgs &a, cudaStream_t s);
 
+// Register-resident FFT kernels for power-of-two lengths 256 .. 4096
+// (gnc_pow2_kernels.cu); the launchers above use them when pow2_fast(size).
+bool pow2_fast(long n);
+cudaError_t launch_rfft_rows_p2(const float *proj, float2 *spec, int T, int H, int W,
+                                cudaStream_t s);
+cudaError_t launch_column_fft_p2(float2 *spec, int T, int H, int W, cudaStream_t s);
+cudaError_t launch_column_flip_p2(const float2 *spec, float2 *g, const int8_t *sign, int t0,
+                                  int nt, int D, int H, int W, cudaStream_t s);
+cudaError_t launch_row_stage_p2(const RowStageArgs &a, cudaStream_t s);
+
 // Exact slab index of the reference (reconstructor.cpp:66-72): the height and
 // defocus coordinate in float without contraction, then
 // floor((double)defocus + 0.5) clamped to [0, D-1].  floor(d + 0.5) equals

@@ -67,6 +67,7 @@ __global__ void k_rfft_rows(const float *__restrict__ proj, float2 *__restrict__
 
 cudaError_t launch_rfft_rows(const float *proj, float2 *spec, int T, int H, int W,
                              cudaStream_t s) {
+  if (pow2_fast(W)) return launch_rfft_rows_p2(proj, spec, T, H, W, s);
   FftPlan plan;
   if (!make_fft_plan(W, &plan)) return cudaErrorInvalidValue;
   int ppb = W >= 4096 ? 1 : 4096 / W;
@@ -122,6 +123,7 @@ __global__ void k_column_fft(float2 *__restrict__ spec, int H, int W, int C, Fft
 }
 
 cudaError_t launch_column_fft(float2 *spec, int T, int H, int W, cudaStream_t s) {
+  if (pow2_fast(H)) return launch_column_fft_p2(spec, T, H, W, s);
   FftPlan plan;
   if (!make_fft_plan(H, &plan)) return cudaErrorInvalidValue;
   const int half = W / 2;
@@ -183,6 +185,7 @@ __global__ void k_column_flip(const float2 *__restrict__ spec, float2 *__restric
 
 cudaError_t launch_column_flip(const float2 *spec, float2 *g, const int8_t *sign, int t0, int nt,
                                int D, int H, int W, cudaStream_t s) {
+  if (pow2_fast(H)) return launch_column_flip_p2(spec, g, sign, t0, nt, D, H, W, s);
   FftPlan plan;
   if (!make_fft_plan(H, &plan)) return cudaErrorInvalidValue;
   const int half = W / 2;

@@ -284,3 +284,52 @@ def test_linearity_at_full_detector_width(torch, oracle):
     va, vb = plan.execute_host(a), plan.execute_host(b)
     vab = plan.execute_host((2.0 * a - 0.5 * b).astype(np.float32))
     assert rel_l2(vab, 2.0 * va - 0.5 * vb) < 1e-5
+
+
+# ------------------------------------------- power-of-two transform lengths
+@pytest.mark.parametrize("staging", ["f32", "f16"])
+@pytest.mark.parametrize("shape", [(5, 256, 1024, 48, 3), (7, 512, 256, 64, 4),
+                                   (3, 1024, 256, 32, 2), (6, 243, 512, 40, 5)])
+def test_pipeline_pow2_sizes_vs_oracles(torch, oracle, staging, shape):
+    T, H, W, Z, D = shape
+    plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=T, H=H, W=W, Z=Z, D=D, staging=staging,
+                                                 seed=11)
+    vol = plan.execute_host(proj)
+    plan.check()
+    if staging == "f32":
+        ref = _oracle_volume(oracle, proj, ang, c, ctf, mn, mx, Z, "f32")
+        assert rel_l2(vol, ref) < FP32_TOL
+    else:
+        ref = _oracle_volume(oracle, proj, ang, c, ctf, mn, mx, Z, "f64")
+        assert rel_l2(vol, ref) < FP16_TOL
+
+
+@pytest.mark.parametrize("W", [256, 512, 2048])
+def test_plain_filter_pow2_vs_oracle(torch, oracle, W):
+    """No CTF: the projections are ramp filtered and backprojected directly."""
+    import guanaco_gb300 as G
+
+    T, H, Z = 9, 6, 40
+    rng = np.random.default_rng(W)
+    ang = np.deg2rad(np.linspace(-60, 60, T)).astype(np.float32)
+    proj = rng.standard_normal((T, H, W)).astype(np.float32)
+    c = G.get_centre(proj.shape, None, False)
+    plan = G.FbpPlan(T, H, W, ang, grid_height=Z, centre=c, correct=False)
+    vol = plan.execute_host(proj)
+    ref = oracle.fbp_ctf(proj, ang, c, 1.0, None, Z=Z)
+    assert rel_l2(vol, ref) < FP32_TOL
+    from guanaco_gb300 import _lib
+
+    rows = rng.standard_normal((3, 4, W)).astype(np.float32)
+    buf = dev(torch, rows)
+    _lib.check(_lib.load().gnc_filter_device(W, 4, 3, buf.data_ptr(), None))
+    assert rel_l2(buf.cpu().numpy(), oracle.ramp_filter(rows)) < 1e-6
+
+
+def test_correct_only_pow2(torch, oracle):
+    plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=3, H=256, W=512, D=4, seed=4)
+    out = torch.empty((plan.T, plan.D, plan.H, plan.W), dtype=torch.float32, device="cuda")
+    plan.correct(dev(torch, proj), out)
+    got = out.cpu().numpy()
+    for t in range(plan.T):
+        assert rel_l2(got[t], oracle.correct(proj[t], ctf)) < 1e-5
