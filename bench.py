@@ -1,0 +1,435 @@
+#!/usr/bin/env python
+"""3D-CTF filtered-backprojection benchmark (one JSON line on stdout).
+
+Workload: 61 tilts over +-60 deg (2 deg steps), 1024 x 1024 projections at
+1.0 A/px, 300 kV, Cs 2.7 mm, defocus 30000 A at the tilt axis, ndf = 10 slabs
+(the reference's default width-based slab range), volume 1024 x 1024 x 300.
+Input: a seeded synthetic phantom of 2000 Gaussian blobs, analytically
+projected and imaged through the CTF at each blob's height (guanaco_gb300.
+synthetic), with Gaussian noise -- the reference publishes no dataset for
+this path.
+
+A step is one whole 3D-CTF FBP of the tilt series: phase-flip correction of
+every tilt into 10 defocus slabs, ramp filtering of every row, backprojection
+of every voxel from every tilt.  The metric is voxel-tilt updates per second
+(Y * Z * X * T per step).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's CPU algorithm (the oracle port,
+oracle/gno_oracle.c, all host threads) on a bounded sample of the same
+workload per step, extrapolated to the whole series.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = ("3D-CTF FBP Gvoxel·tilt/s, FP16-staged vs FP32 at rel-L2≤1e-3; "
+          "serve p50/p99 ms")
+UNIT = "Gvoxel·tilt/s"
+WL = dict(T=61, H=1024, W=1024, Z=300, D=10, pixel_size=1.0, defocus=30000.0, energy=300.0,
+          cs_mm=2.7, blobs=2000, seed=3, tilt_max=60.0, noise=0.1)
+WORKLOAD_NAME = ("3D CTF ndf=10: 61 tilts +-60 deg, 1024x1024 projections at 1.0 A/px, "
+                 "300 kV, Cs 2.7 mm, df 30000 A, volume 1024x1024x300")
+# DRAM traffic of one k_bp_fast launch on this workload, from the ncu capture
+# summarised in profiles/k_bp_fast_3dctf_ndf10.md (bytes read + written).
+BP_TRAFFIC_BYTES = {"f32": None, "f16": None}
+
+
+def angles_rad():
+    n = WL["T"]
+    return np.deg2rad(np.linspace(-WL["tilt_max"], WL["tilt_max"], n)).astype(np.float32)
+
+
+def voxel_tilts():
+    return WL["H"] * WL["Z"] * WL["W"] * WL["T"]
+
+
+def slab_setup():
+    import guanaco_gb300 as G
+
+    c = G.get_centre((WL["T"], WL["H"], WL["W"]), None, False)
+    mn, mx, step, nd = G.get_defocus_steps(WL["defocus"], WL["D"], None, WL["W"], c,
+                                           WL["pixel_size"])
+    return c, mn, mx, step, nd
+
+
+def make_plan(staging):
+    import guanaco_gb300 as G
+
+    c, mn, mx, step, nd = slab_setup()
+    df = WL["defocus"]
+    return G.FbpPlan(WL["T"], WL["H"], WL["W"], angles_rad(), grid_height=WL["Z"],
+                     grid_width=WL["W"], centre=c, pixel_size=WL["pixel_size"], input="raw",
+                     correct=True, num_defocus=nd, slab_defocus=G.api.slab_defoci(mn, nd, step),
+                     min_defocus=float(mn - df), max_defocus=float(mx - df), energy=WL["energy"],
+                     spherical_aberration=WL["cs_mm"], staging=staging)
+
+
+def make_projections(device):
+    from guanaco_gb300 import synthetic
+
+    blobs = synthetic.blob_phantom(WL["blobs"], WL["W"], WL["H"], WL["Z"], WL["seed"])
+    return synthetic.tilt_series(blobs, angles_rad(), WL["H"], WL["W"],
+                                 pixel_size=WL["pixel_size"], defocus=WL["defocus"],
+                                 energy=WL["energy"], cs_mm=WL["cs_mm"], noise=WL["noise"],
+                                 seed=WL["seed"], device=device)
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200", "-f", self.path],
+                stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    smax.append(float(p[2]))
+                except ValueError:
+                    continue
+                for name, v in zip(names, p[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------- our arm
+def run_ours(args, rank, world, dist):
+    import torch
+
+    import guanaco_gb300 as G  # noqa: F401
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    proj = make_projections(dev)
+    torch.cuda.synchronize()
+    plans = {"f32": make_plan("f32"), "f16": make_plan("f16")}
+    vols = {k: torch.empty((WL["H"], WL["Z"], WL["W"]), dtype=torch.float32, device=dev)
+            for k in plans}
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(form):
+        plan, vol = plans[form], vols[form]
+        for _ in range(args.warmup):
+            plan.execute(proj, vol, stream)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * args.steps + 2)]
+        barrier()
+        ev[0].record(stream)
+        for k in range(args.steps):
+            plan.stage(proj, stream)
+            ev[2 * k + 1].record(stream)
+            plan.backproject(vol, False, stream)
+            ev[2 * k + 2].record(stream)
+        ev[-1].record(stream)
+        barrier()
+        total = ev[0].elapsed_time(ev[-1])
+        bp = [ev[2 * k + 1].elapsed_time(ev[2 * k + 2]) for k in range(args.steps)]
+        plan.check(stream)
+        return total, sum(bp) / len(bp)
+
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    res = {form: timed(form) for form in ("f32", "f16")}
+    # end to end through the public host-buffer entry point: pinned input in,
+    # volume out, every step
+    h_in = torch.empty(proj.shape, dtype=torch.float32, pin_memory=True)
+    h_in.copy_(proj)
+    h_in_np = h_in.numpy()
+    h_out = torch.empty((WL["H"], WL["Z"], WL["W"]), dtype=torch.float32, pin_memory=True)
+    h_out_np = h_out.numpy()
+    plans["f32"].execute_host(h_in_np, h_out_np, stream)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        plans["f32"].execute_host(h_in_np, h_out_np, stream)
+    barrier()
+    e2e_ms = (time.perf_counter() - t0) * 1e3
+    clk = clocks.stop()
+
+    def reduce_max(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    total32 = reduce_max(res["f32"][0])
+    total16 = reduce_max(res["f16"][0])
+    e2e_ms = reduce_max(e2e_ms)
+    units = voxel_tilts() * args.steps * world
+    value32 = units / (total32 * 1e-3) / 1e9
+    value16 = units / (total16 * 1e-3) / 1e9
+    e2e_value = units / (e2e_ms * 1e-3) / 1e9
+
+    parity = cpu = None
+    if rank == 0 and not args.no_cpu:
+        parity, cpu = oracle_sample(proj, vols)
+    if rank != 0:
+        return
+    import json as _json
+
+    peaks = {}
+    try:
+        peaks = _json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    p32 = plans["f32"]
+    staged_bytes = WL["D"] * WL["T"] * WL["H"] * WL["W"] * 4
+    vol_bytes = WL["H"] * WL["Z"] * WL["W"] * 4
+    bp_alg = staged_bytes + vol_bytes
+    bp_ms = res["f32"][1]
+    achieved = bp_alg / (bp_ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC,
+        "value": round(value32, 2),
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(total32 / args.steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic: 2000-blob phantom, analytic projections through the CTF, seeded",
+        "config": {
+            "workload": WORKLOAD_NAME,
+            "tilts": WL["T"], "projection": [WL["H"], WL["W"]], "volume": [WL["H"], WL["W"], WL["Z"]],
+            "ndf": WL["D"], "staging": "f32", "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2: 256 MB projections, 2.6 GB staged rows per step",
+        },
+        "forms": {
+            "f32": {"value": round(value32, 2), "ms_per_step": round(total32 / args.steps, 4),
+                    "bp_ms": round(res["f32"][1], 4)},
+            "f16": {"value": round(value16, 2), "ms_per_step": round(total16 / args.steps, 4),
+                    "bp_ms": round(res["f16"][1], 4),
+                    "speedup_vs_f32": round(value16 / value32, 3)},
+        },
+        "e2e": {
+            "value": round(e2e_value, 2), "unit": UNIT,
+            "h2d_bytes_per_step": int(proj.numel() * 4),
+            "d2h_bytes_per_step": int(WL["H"] * WL["Z"] * WL["W"] * 4),
+            "ms_per_step": round(e2e_ms / args.steps, 4),
+            "api": "gnc_fbp_execute_host (pinned host buffers)",
+        },
+        "roofline": {
+            "kernel": "k_bp_fast (backprojection)",
+            "bound": "hbm",
+            "achieved": round(achieved, 1),
+            "peak": hbm_peak,
+            "peak_source": peak_src,
+            "unit": "GB/s",
+            "frac": round(achieved / hbm_peak, 4),
+            "traffic": BP_TRAFFIC_BYTES["f32"],
+            "algorithmic_bytes": bp_alg,
+            "kernel_ms": round(bp_ms, 4),
+        },
+        "clocks": clk,
+        # kernels of this library launched in the timed region of `value`
+        "gpu_launches": int(p32.launches_per_execute * args.steps),
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    if parity is not None:
+        line["parity"] = parity
+    print(json.dumps(line))
+
+
+def oracle_sample(proj, vols, nrows=8):
+    """FP32 and FP64 oracle on a sample of rows of the same series: parity of
+    both GPU forms, and the timed CPU baseline (correction of every tilt plus
+    filter and backprojection of the sampled rows, extrapolated)."""
+    from oracle import oracle as O
+
+    c, mn, mx, step, nd = slab_setup()
+    df = WL["defocus"]
+    ctf = O.ctf_stack(WL["W"], WL["H"], WL["pixel_size"], WL["energy"], mn, nd, step, WL["cs_mm"])
+    p = proj.cpu().numpy()
+    ang = angles_rad()
+    y0 = WL["H"] // 2 - nrows // 2
+    rows = (y0, y0 + nrows)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    O.fbp_ctf(p, ang, c, WL["pixel_size"], ctf, float(mn - df), float(mx - df), Z=WL["Z"],
+              rows=(0, 0), nthreads=threads)
+    t_corr = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    v32 = O.fbp_ctf(p, ang, c, WL["pixel_size"], ctf, float(mn - df), float(mx - df), Z=WL["Z"],
+                    rows=rows, nthreads=threads)
+    t_both = time.perf_counter() - t0
+    t_rows = max(t_both - t_corr, 1e-9)
+    v64 = O.fbp_ctf(p, ang, c, WL["pixel_size"], ctf, float(mn - df), float(mx - df), Z=WL["Z"],
+                    rows=rows, precision="f64", nthreads=threads)
+    sl = slice(*rows)
+    r64 = v64[sl]
+    r32 = v32[sl]
+
+    def rel(a, b):
+        return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
+
+    g32 = vols["f32"][sl].cpu().numpy()
+    g16 = vols["f16"][sl].cpu().numpy()
+    parity = {
+        "rows_sampled": list(rows),
+        "f32_vs_reference_cpu_rel_l2": rel(g32, r32),
+        "f32_vs_fp64_oracle_rel_l2": rel(g32, r64),
+        "f16_vs_fp64_oracle_rel_l2": rel(g16, r64),
+        "f32_max_abs_vs_fp64": float(np.abs(g32 - r64).max()),
+        "reference_cpu_vs_fp64_rel_l2": rel(r32, r64),
+    }
+    full_s = t_corr + t_rows * WL["H"] / nrows
+    cpu = {
+        "value": round(voxel_tilts() / full_s / 1e9, 4),
+        "unit": UNIT,
+        "cores": threads,
+        "kind": "port",
+        "sample": (f"oracle restatement of the reference CPU path (float, OpenMP, {threads} "
+                   f"threads): CTF correction of all {WL['T']} tilts ({t_corr:.2f} s) plus "
+                   f"filter and backprojection of {nrows} of {WL['H']} rows ({t_rows:.2f} s), "
+                   f"extrapolated to all rows: {full_s:.1f} s per series"),
+    }
+    return parity, cpu
+
+
+# ------------------------------------------------------------ reference arm
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    import guanaco_gb300 as G  # noqa: F401  (host helpers only: defocus steps)
+
+    threads = os.cpu_count() or 1
+    c, mn, mx, step, nd = slab_setup()
+    df = WL["defocus"]
+    rng = np.random.default_rng(WL["seed"])
+    # the sample needs only its tilts and rows: a seeded stand-in with the
+    # workload's shape (the timing does not depend on the values)
+    p = rng.standard_normal((WL["T"], WL["H"], WL["W"])).astype(np.float32)
+    ctf = O.ctf_stack(WL["W"], WL["H"], WL["pixel_size"], WL["energy"], mn, nd, step, WL["cs_mm"])
+    ang = angles_rad()
+    k_tilts = min(WL["T"], threads)
+    m_rows = threads
+
+    def step_once():
+        t0 = time.perf_counter()
+        O.fbp_ctf(p, ang, c, WL["pixel_size"], ctf, float(mn - df), float(mx - df), Z=WL["Z"],
+                  rows=(0, 0), tilts=(0, k_tilts), nthreads=threads)
+        t1 = time.perf_counter()
+        O.fbp_ctf(p, ang, c, WL["pixel_size"], ctf, float(mn - df), float(mx - df), Z=WL["Z"],
+                  rows=(0, m_rows), tilts=(0, 0), nthreads=threads)
+        t2 = time.perf_counter()
+        return (t1 - t0) * WL["T"] / k_tilts + (t2 - t1) * WL["H"] / m_rows
+
+    for _ in range(args.warmup):
+        step_once()
+    per = [step_once() for _ in range(args.steps)]
+    full_s = sum(per) / len(per)
+    value = voxel_tilts() / full_s / 1e9
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "impl": "reference",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(full_s * 1e3, 2), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, workload shape)",
+        "config": {"workload": WORKLOAD_NAME, "tilts": WL["T"],
+                   "projection": [WL["H"], WL["W"]], "volume": [WL["H"], WL["W"], WL["Z"]],
+                   "ndf": WL["D"], "staging": "f32", "parallelism": "host threads"},
+        "cpu_baseline": {
+            "value": round(value, 4), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": (f"per step: CTF correction of {k_tilts} of {WL['T']} tilts and filter + "
+                       f"backprojection of {m_rows} of {WL['H']} rows, extrapolated to the "
+                       "whole series; oracle restatement of the reference CPU path (the "
+                       "reference itself needs FFTW and its source tree, absent on this host)"),
+        },
+        "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the oracle parity/CPU sample")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        tdist.init_process_group("nccl")
+        dist = tdist
+    try:
+        run_ours(args, rank, world, dist)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -116,6 +116,7 @@ SIGNATURES = {
     "gnc_fbp_sign_table": (c_int, [c_void, c_void, c_void]),
     "gnc_fbp_staged": (c_int, [c_void, ctypes.POINTER(c_void), ctypes.POINTER(c_void)]),
     "gnc_fbp_check": (c_int, [c_void, c_void]),
+    "gnc_fbp_launches": (c_int, [c_void]),
 }
 
 

@@ -459,6 +459,13 @@ int gnc_fbp_slab_map(gnc_fbp_plan *p, int32_t *d_out, void *stream) {
   return GNC_OK;
 }
 
+int gnc_fbp_launches(const gnc_fbp_plan *p) {
+  if (!p) return 0;
+  if (!p->correct) return 2;  // row stage, backprojection
+  const int chunks = (p->T + p->chunk - 1) / p->chunk;
+  return 3 + 2 * chunks + 1;  // sign table, row and column transforms, per chunk flip + rows, BP
+}
+
 int gnc_fbp_check(gnc_fbp_plan *p, void *stream) {
   GNC_REQUIRE(p != nullptr);
   int h = 0;

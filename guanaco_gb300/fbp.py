@@ -115,6 +115,10 @@ class FbpPlan:
         return self._lib.gnc_fbp_workspace_bytes(self._h)
 
     @property
+    def launches_per_execute(self):
+        return self._lib.gnc_fbp_launches(self._h)
+
+    @property
     def voxel_tilts(self):
         return self.H * self.Z * self.X * self.T
 

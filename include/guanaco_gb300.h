@@ -199,6 +199,8 @@ GNC_API int gnc_fbp_backproject_staged(gnc_fbp_plan *plan, const void *d_staged,
 GNC_API int gnc_fbp_slab_map(gnc_fbp_plan *plan, int32_t *d_out, void *stream);
 /* int8 (D, H, W/2 + 1) table of s(k) + s(-k) with s the phase-flip factor. */
 GNC_API int gnc_fbp_sign_table(gnc_fbp_plan *plan, int8_t *d_out, void *stream);
+/* Number of kernel launches one gnc_fbp_execute enqueues. */
+GNC_API int gnc_fbp_launches(const gnc_fbp_plan *plan);
 /* Synchronises `stream` and reports (then clears) a device-side error of the
  * plan's kernels: every wait in them is bounded and records a timeout here
  * instead of hanging. */

@@ -413,7 +413,7 @@ void gno_fbp_ctf_f(const float *proj, size_t T, size_t H, size_t W, const float 
 void gno_fbp_ctf_d(const float *proj, size_t T, size_t H, size_t W, const float *angles,
                    const float *centre, float pixel_size, const float *ctf, size_t D,
                    float min_defocus, float max_defocus, const double *weights, int minus,
-                   size_t Z, double *vol, int nthreads) {
+                   size_t Z, double *vol, size_t y_begin, size_t y_end, int nthreads) {
   set_threads(nthreads);
   size_t nd = D > 0 ? D : 1;
   size_t img = H * W;
@@ -430,7 +430,7 @@ void gno_fbp_ctf_d(const float *proj, size_t T, size_t H, size_t W, const float 
     for (size_t k = 0; k < T * img; ++k) stack[k] = (double)proj[k];
   }
 #pragma omp parallel for schedule(dynamic, 1)
-  for (long yy = 0; yy < (long)H; ++yy) {
+  for (long yy = (long)y_begin; yy < (long)y_end; ++yy) {
     size_t y = (size_t)yy;
     double *sino = (double *)malloc(nd * T * W * sizeof(double));
     for (size_t d = 0; d < nd; ++d)

@@ -106,7 +106,7 @@ void gno_fbp_ctf_f(const float *proj, size_t T, size_t H, size_t W, const float 
 void gno_fbp_ctf_d(const float *proj, size_t T, size_t H, size_t W, const float *angles,
                    const float *centre, float pixel_size, const float *ctf, size_t D,
                    float min_defocus, float max_defocus, const double *weights, int minus,
-                   size_t Z, double *vol, int nthreads);
+                   size_t Z, double *vol, size_t y_begin, size_t y_end, int nthreads);
 
 #ifdef __cplusplus
 }

@@ -87,7 +87,7 @@ def lib():
                                     _sz, _sz, _sz, _sz, ctypes.c_int]
         L.gno_fbp_ctf_d.argtypes = [_f32p, _sz, _sz, _sz, _f32p, _f32p, ctypes.c_float, vp, _sz,
                                     ctypes.c_float, ctypes.c_float, vp, ctypes.c_int, _sz, _f64p,
-                                    ctypes.c_int]
+                                    _sz, _sz, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -248,8 +248,9 @@ def fbp_ctf(proj, angles, centre, pixel_size, ctf=None, min_defocus=0.0, max_def
     """Whole pipeline on (T, H, W) projections -> (H, Z, W) volume.
 
     ``ctf`` is the complex64 (D, H, W) stack from :func:`ctf_stack` or None
-    (no correction).  ``rows``/``tilts`` restrict the float pipeline to a
-    sample of rows / corrected tilts (timing only)."""
+    (no correction).  ``rows`` restricts the backprojection to a sample of Y
+    rows (both precisions); ``tilts`` restricts the float pipeline's
+    correction to a sample of tilts (timing only)."""
     proj = np.ascontiguousarray(proj, dtype=np.float32)
     T, H, W = proj.shape
     Z = W if Z is None else Z
@@ -274,7 +275,8 @@ def fbp_ctf(proj, angles, centre, pixel_size, ctf=None, min_defocus=0.0, max_def
                             vol, y0, y1, t0, t1, int(nthreads))
     else:
         vol = np.zeros((H, Z, W), dtype=np.float64)
+        y0, y1 = (0, H) if rows is None else rows
         lib().gno_fbp_ctf_d(proj, T, H, W, angles, centre, float(pixel_size), cptr, D,
                             float(min_defocus), float(max_defocus), wptr, int(bool(minus)), Z,
-                            vol, int(nthreads))
+                            vol, y0, y1, int(nthreads))
     return vol
