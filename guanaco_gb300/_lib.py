@@ -91,6 +91,8 @@ SIGNATURES = {
     "gnc_version": (c_int, []),
     "gnc_reconstruct": (c_int, [ctypes.POINTER(GncConfig), c_void, c_void]),
     "gnc_reconstruct_device": (c_int, [ctypes.POINTER(GncConfig), c_void, c_void, c_void]),
+    "gnc_reconstruct_device_noalloc": (c_int, [ctypes.POINTER(GncConfig), c_void, c_void,
+                                               c_void]),
     "gnc_filter_device": (c_int, [c_size, c_size, c_size, c_void, c_void]),
     "gnc_correct": (c_int, [c_void, c_void, c_void, c_size, c_size, c_size]),
     "gnc_get_electron_wavelength": (c_double, [c_double]),

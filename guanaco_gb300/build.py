@@ -29,6 +29,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
 EXTRA = {
     "gnc_ctf.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
     "gnc_api.cu": ["-Xcompiler", "-ffp-contract=off"],
+    "gnc_noalloc.cu": ["-Xcompiler", "-ffp-contract=off"],
 }
 
 

@@ -77,6 +77,20 @@ GNC_API int gnc_reconstruct(const gnc_config *config, const float *sinogram,
 GNC_API int gnc_reconstruct_device(const gnc_config *config, const float *d_sinogram,
                                    float *d_reconstruction, void *stream);
 
+/* No counterpart in the reference.  gnc_reconstruct_device without any device
+ * allocation, for callers that cannot allocate inside a call: an application
+ * that owns a fixed device-memory budget, a real-time loop that must not touch
+ * the allocator, or work being recorded into a CUDA graph.  Its scratch lives
+ * in static device arrays (about 16.1 MiB held by every GPU that loads the
+ * library until exit).  Limits: num_defocus * num_angles * num_pixels <=
+ * 4194304, num_angles <= 1024, num_pixels <= 4096; larger requests return
+ * GNC_ERR_INVALID_ARGUMENT.  All calls on a device share the scratch, so calls
+ * that overlap on the GPU race; serialise them.  The first call on a device
+ * looks the scratch up (cudaGetSymbolAddress) and should come before any
+ * stream capture. */
+GNC_API int gnc_reconstruct_device_noalloc(const gnc_config *config, const float *d_sinogram,
+                                           float *d_reconstruction, void *stream);
+
 /* guanaco::Filter<e_device>(num_pixels, num_angles, num_defocus)(data)
  * (include/guanaco/filter.h:32-54, src/libguanaco/filter.cu:144-202): ramp
  * filter of D*T rows of N pixels in place, device pointer. */
