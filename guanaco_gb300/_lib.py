@@ -82,6 +82,7 @@ class GncFbpDesc(ctypes.Structure):
         ("weights", ctypes.POINTER(c_double)),
         ("minus", c_int),
         ("staging", c_int),
+        ("ctf_pixel_size", c_double),
     ]
 
 

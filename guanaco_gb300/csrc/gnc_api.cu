@@ -273,13 +273,14 @@ int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
     p->sargs.D = p->D;
     p->sargs.H = p->H;
     p->sargs.W = p->W;
-    p->sargs.inv_ps = 1.0 / (double)d->pixel_size;
+    p->sargs.inv_ps = 1.0 / (d->ctf_pixel_size > 0 ? d->ctf_pixel_size : (double)d->pixel_size);
     p->sargs.l = gnc_get_electron_wavelength(d->energy_kev * 1000);
     p->sargs.Cs = d->cs_mm * 1e7;
     p->sargs.Ca = d->astigmatism;
     p->sargs.Pa = d->astigmatism_angle_deg * M_PI / 180;
     p->sargs.phi = d->phase_shift_deg * M_PI / 180;
     p->sargs.slab_df = p->slab_df;
+    fill_sign_screen(&p->sargs);
   }
   // +8 pixels: a 16-byte aligned bulk copy of the last row may run past its end
   const size_t elems = (size_t)p->Y2 * p->D * p->T * p->W + 8;

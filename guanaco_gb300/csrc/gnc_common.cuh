@@ -53,12 +53,16 @@ cudaError_t launch_column_flip(const float2 *spec, float2 *g, const int8_t *sign
 
 // The 2 * symmetrised phase-flip sign for every (slab, ky, kx <= W/2), from the
 // FP64 CTF phase (include/guanaco/ctf.h:88-101, 233-273; correct.h:30-39).
+// The kernel first screens each sign in float (fill_sign_screen sets the f_*
+// fields) and evaluates the FP64 phase only where the screen cannot decide.
 struct SignTableArgs {
   int D, H, W;
   double inv_ps;
   double l, Cs, Ca, Pa, phi;
   const double *slab_df;  // device, D
+  float f_a4, f_phipi, f_c2p, f_s2p, f_ips2, f_lca;
 };
+void fill_sign_screen(SignTableArgs *a);
 cudaError_t launch_sign_table(const SignTableArgs &a, int8_t *out, cudaStream_t s);
 
 // Row stage.  Input rows come either from the column stage (packed half
@@ -131,6 +135,14 @@ cudaError_t launch_column_fft_p2(float2 *spec, int T, int H, int W, cudaStream_t
 cudaError_t launch_column_flip_p2(const float2 *spec, float2 *g, const int8_t *sign, int t0,
                                   int nt, int D, int H, int W, cudaStream_t s);
 cudaError_t launch_row_stage_p2(const RowStageArgs &a, cudaStream_t s);
+
+// One-warp register FFT kernels for 1024-point rows / columns
+// (gnc_w1024_kernels.cu); the launchers above prefer them for that size.
+cudaError_t launch_rfft_rows_w1024(const float *proj, float2 *spec, int T, int H, cudaStream_t s);
+cudaError_t launch_column_fft_w1024(float2 *spec, int T, int W, cudaStream_t s);
+cudaError_t launch_column_flip_w1024(const float2 *spec, float2 *g, const int8_t *sign, int t0,
+                                     int nt, int D, int W, cudaStream_t s);
+cudaError_t launch_row_stage_w1024(const RowStageArgs &a, cudaStream_t s);
 
 // Exact slab index of the reference (reconstructor.cpp:66-72): the height and
 // defocus coordinate in float without contraction, then

@@ -67,6 +67,7 @@ __global__ void k_rfft_rows(const float *__restrict__ proj, float2 *__restrict__
 
 cudaError_t launch_rfft_rows(const float *proj, float2 *spec, int T, int H, int W,
                              cudaStream_t s) {
+  if (W == 1024) return launch_rfft_rows_w1024(proj, spec, T, H, s);
   if (pow2_fast(W)) return launch_rfft_rows_p2(proj, spec, T, H, W, s);
   FftPlan plan;
   if (!make_fft_plan(W, &plan)) return cudaErrorInvalidValue;
@@ -123,6 +124,7 @@ __global__ void k_column_fft(float2 *__restrict__ spec, int H, int W, int C, Fft
 }
 
 cudaError_t launch_column_fft(float2 *spec, int T, int H, int W, cudaStream_t s) {
+  if (H == 1024) return launch_column_fft_w1024(spec, T, W, s);
   if (pow2_fast(H)) return launch_column_fft_p2(spec, T, H, W, s);
   FftPlan plan;
   if (!make_fft_plan(H, &plan)) return cudaErrorInvalidValue;
@@ -185,6 +187,7 @@ __global__ void k_column_flip(const float2 *__restrict__ spec, float2 *__restric
 
 cudaError_t launch_column_flip(const float2 *spec, float2 *g, const int8_t *sign, int t0, int nt,
                                int D, int H, int W, cudaStream_t s) {
+  if (H == 1024) return launch_column_flip_w1024(spec, g, sign, t0, nt, D, W, s);
   if (pow2_fast(H)) return launch_column_flip_p2(spec, g, sign, t0, nt, D, H, W, s);
   FftPlan plan;
   if (!make_fft_plan(H, &plan)) return cudaErrorInvalidValue;

@@ -27,7 +27,7 @@ __host__ __device__ inline double chi(double l, double df0, double Cs, double Ca
 
 // The reference stores exp(-i(chi - phi)) as complex64 (correct.py:192-211)
 // and phase_flip multiplies by -sign(imag) (correct.h:30-39).
-__device__ inline int flip_sign(double l, double df, double Cs, double Ca, double Pa, double phi,
+__host__ __device__ inline int flip_sign(double l, double df, double Cs, double Ca, double Pa, double phi,
                                 long x, long y, long w, long h, double inv_ps) {
   double q, theta;
   r_and_theta(x, y, w, h, inv_ps, Ca != 0.0, &q, &theta);
@@ -36,35 +36,85 @@ __device__ inline int flip_sign(double l, double df, double Cs, double Ca, doubl
   return -((0.0f < im) - (im < 0.0f));
 }
 
+// Float screen for the sign.  With u = a / pi,
+//   u = l df q^2 - (Cs l^3 / 2) q^4 + phi / pi,
+//   l df q^2 = l df0 q^2 + l Ca inv_ps^2 (cos 2Pa (dx^2 - dy^2) + sin 2Pa 2 dx dy)
+// (cos(2 (theta - Pa)) expanded with cos 2theta = (dx^2 - dy^2) / r^2 and
+// sin 2theta = 2 dx dy / r^2, so no transcendental is needed), and
+// -sign(sin(pi u)) is +1 when floor(u) is odd and -1 when it is even.  The
+// float value of u carries at most a few ulps of each term; when it lies within
+// kScreen * (sum of the terms' magnitudes) + kScreenAbs of an integer the FP64
+// evaluation above decides instead, so every sign equals the FP64 one.
+constexpr float kScreen = 4e-6f, kScreenAbs = 1e-6f;
+
+// FFT-ordered frequency coordinate of bin x (0 <= x < w) in float.
+__host__ __device__ inline float fft_coord(int x, int w) {
+  const int w2 = w / 2;
+  int c = x + w2;
+  c -= c >= w ? w : 0;
+  return (float)(c - w2) / (float)w;
+}
+
+__host__ __device__ inline int screened_sign(const SignTableArgs &p, float ldf, int x, int y, bool *sure) {
+  const float dx = fft_coord(x, p.W), dy = fft_coord(y, p.H);
+  const float xx = dx * dx, yy = dy * dy, xy = 2.0f * dx * dy;
+  const float q2 = (xx + yy) * p.f_ips2;
+  const float t0 = ldf * q2;
+  const float ta = p.f_lca * (p.f_c2p * (xx - yy) + p.f_s2p * xy);
+  const float t4 = p.f_a4 * q2 * q2;
+  const float u = t0 + ta - t4 + p.f_phipi;
+  const float mag = fabsf(t0) + fabsf(p.f_lca) * (fabsf(xx - yy) + fabsf(xy)) + fabsf(t4) +
+                    fabsf(p.f_phipi);
+  const float fl = floorf(u);
+  // within an ulp of 1 of the exact fraction (exact for u >= 0), far below the margin
+  const float fr = u - fl;
+  const float margin = kScreen * mag + kScreenAbs;
+  *sure = fr > margin && fr < 1.0f - margin && fabsf(u) < 4.0e6f;
+  return ((int)fl & 1) ? 1 : -1;
+}
+
+// One block per (slab, ky) row of the table at a time.
 __global__ void k_sign_table(SignTableArgs a, int8_t *__restrict__ out) {
-  const int half = a.W / 2;
-  const int sw = half + 1;
-  const long total = (long)a.D * a.H * sw;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total;
-       i += (long)gridDim.x * blockDim.x) {
-    int kx = (int)(i % sw);
-    long r = i / sw;
-    int ky = (int)(r % a.H);
-    int d = (int)(r / a.H);
-    double df = a.slab_df[d];
-    int s0 = flip_sign(a.l, df, a.Cs, a.Ca, a.Pa, a.phi, kx, ky, a.W, a.H, a.inv_ps);
-    int s1;
-    if (a.Ca == 0.0) {
-      // without astigmatism q(-k) == q(k) bit for bit, so s(-k) == s(k)
-      s1 = s0;
-    } else {
-      s1 = flip_sign(a.l, df, a.Cs, a.Ca, a.Pa, a.phi, (a.W - kx) % a.W, (a.H - ky) % a.H, a.W,
-                     a.H, a.inv_ps);
+  const int sw = a.W / 2 + 1;
+  const long rows = (long)a.D * a.H;
+  for (long row = blockIdx.x; row < rows; row += gridDim.x) {
+    const int d = (int)(row / a.H);
+    const int ky = (int)(row - (long)d * a.H);
+    const double df = a.slab_df[d];
+    const float ldf = (float)(a.l * df);
+    int8_t *o = out + row * sw;
+    for (int kx = threadIdx.x; kx < sw; kx += blockDim.x) {
+      bool sure;
+      int s0 = screened_sign(a, ldf, kx, ky, &sure);
+      if (!sure) s0 = flip_sign(a.l, df, a.Cs, a.Ca, a.Pa, a.phi, kx, ky, a.W, a.H, a.inv_ps);
+      int s1;
+      if (a.Ca == 0.0) {
+        // without astigmatism q(-k) == q(k) bit for bit, so s(-k) == s(k)
+        s1 = s0;
+      } else {
+        const int mx = kx == 0 ? 0 : a.W - kx, my = ky == 0 ? 0 : a.H - ky;
+        s1 = screened_sign(a, ldf, mx, my, &sure);
+        if (!sure) s1 = flip_sign(a.l, df, a.Cs, a.Ca, a.Pa, a.phi, mx, my, a.W, a.H, a.inv_ps);
+      }
+      o[kx] = (int8_t)(s0 + s1);
     }
-    out[i] = (int8_t)(s0 + s1);
   }
 }
 
+void fill_sign_screen(SignTableArgs *a) {
+  a->f_a4 = (float)(a->Cs * a->l * a->l * a->l / 2);
+  a->f_phipi = (float)(a->phi / M_PI);
+  a->f_c2p = (float)cos(2 * a->Pa);
+  a->f_s2p = (float)sin(2 * a->Pa);
+  a->f_ips2 = (float)(a->inv_ps * a->inv_ps);
+  a->f_lca = (float)(a->l * a->Ca * a->inv_ps * a->inv_ps);
+}
+
 cudaError_t launch_sign_table(const SignTableArgs &a, int8_t *out, cudaStream_t s) {
-  long total = (long)a.D * a.H * (a.W / 2 + 1);
-  int blocks = (int)((total + 255) / 256);
-  if (blocks > 152 * 32) blocks = 152 * 32;
-  k_sign_table<<<blocks, 256, 0, s>>>(a, out);
+  const long rows = (long)a.D * a.H;
+  const int threads = a.W / 2 + 1 >= 256 ? 256 : 128;
+  const int blocks = (int)(rows < 152 * 16 ? rows : 152 * 16);
+  k_sign_table<<<blocks, threads, 0, s>>>(a, out);
   return cudaGetLastError();
 }
 

@@ -78,6 +78,7 @@ class FbpPlan:
         d.centre = (None if self._centre is None
                     else self._centre.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
         d.pixel_size = float(pixel_size)
+        d.ctf_pixel_size = float(pixel_size)
         d.input = _lib.GNC_INPUT_RAW if input == "raw" else _lib.GNC_INPUT_CORRECTED
         d.correct = 1 if (correct and input == "raw") else 0
         d.num_defocus = self.D

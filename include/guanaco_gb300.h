@@ -183,6 +183,9 @@ typedef struct {
   const double *weights; /* host, T per-tilt weights (mp.py:135-141) or NULL */
   int minus;             /* transform == "minus" (mp.py:128-129) */
   int staging;           /* GNC_STAGE_F32 or GNC_STAGE_F16 */
+  double ctf_pixel_size; /* A, for the CTF only, in double as the reference's CTF
+                            takes it (src/guanaco/detail/ext/ctf.h:142-149);
+                            0 = pixel_size */
 } gnc_fbp_desc;
 
 /* Allocates the plan's device workspace on the current device. */

@@ -156,6 +156,19 @@ def test_sign_table_bit_exact(torch, oracle, Ca, phi, ps):
     np.testing.assert_array_equal(out.cpu().numpy(), _sym_sign(ctf))
 
 
+# Full-size tables: millions of signs, many near a sign change, where the float
+# screen has to hand over to the FP64 phase.
+@pytest.mark.parametrize("H,W,D,Ca,phi,ps,df", [(1024, 1024, 10, 0.0, 0.0, 1.0, 30000.0),
+                                                (384, 512, 6, 600.0, 2.0, 0.8, 20000.0),
+                                                (243, 500, 5, 300.0, 7.0, 1.3, 40000.0)])
+def test_sign_table_bit_exact_large(torch, oracle, H, W, D, Ca, phi, ps, df):
+    plan, proj, *_, ctf, mn, mx = _plan_case(oracle, T=3, H=H, W=W, Z=8, D=D, ps=ps, Ca=Ca,
+                                             phi=phi, df=df)
+    out = torch.empty((plan.D, plan.H, plan.W // 2 + 1), dtype=torch.int8, device="cuda")
+    plan.sign_table(out)
+    np.testing.assert_array_equal(out.cpu().numpy(), _sym_sign(ctf))
+
+
 @pytest.mark.parametrize("D,Z", [(5, 40), (10, 33), (3, 64)])
 def test_slab_map_bit_exact(torch, oracle, D, Z):
     plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, D=D, Z=Z)
