@@ -46,7 +46,7 @@ WORKLOAD_NAME = ("3D CTF ndf=10: 61 tilts +-60 deg, 1024x1024 projections at 1.0
                  "300 kV, Cs 2.7 mm, df 30000 A, volume 1024x1024x300")
 # DRAM traffic of one k_bp_fast launch on this workload, from the ncu capture
 # summarised in profiles/k_bp_fast_3dctf_ndf10.md (bytes read + written).
-BP_TRAFFIC_BYTES = {"f32": None, "f16": None}
+BP_TRAFFIC_BYTES = {"f32": 2.31e9, "f16": 1.767e9}
 
 
 def angles_rad():
@@ -409,7 +409,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the oracle parity/CPU sample")
+    ap.add_argument("--case", choices=["3dctf", "profile"], default="3dctf",
+                    help="profile: the same 1024^2 ndf=10 kernels on 16 tilts and a 64-voxel-"
+                         "thick volume, small enough for ncu captures (not a bench line)")
     args = ap.parse_args()
+    if args.case == "profile":
+        global WORKLOAD_NAME
+        WL.update(T=16, Z=64, blobs=200)
+        WORKLOAD_NAME = "profiling case: " + WORKLOAD_NAME.replace("61 tilts", "16 tilts").replace(
+            "x300", "x64")
+        args.no_cpu = True
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

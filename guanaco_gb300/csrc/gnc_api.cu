@@ -131,6 +131,10 @@ using namespace gnc;
   } while (0)
 
 // ------------------------------------------------------------- the plan ----
+// Host-buffer pipeline: input copies in up to kIoGroups tilt groups, volume
+// copies out in up to kIoSlabs row slabs, plus two events for the stream joins.
+constexpr int kIoGroups = 32, kIoSlabs = 8, kIoEvents = kIoGroups + kIoSlabs + 2;
+
 struct gnc_fbp_plan {
   int device = 0;
   int T = 0, H = 0, W = 0, Z = 0, X = 0, D = 1, Y2 = 0;
@@ -151,6 +155,10 @@ struct gnc_fbp_plan {
   float *tilt_factor = nullptr;
   int *err = nullptr;        // device error word of the bounded waits
   size_t bytes = 0;
+  // host-buffer path (gnc_fbp_execute_host), created on its first call
+  float *io_in = nullptr, *io_out = nullptr;
+  cudaStream_t s_in = nullptr, s_out = nullptr;
+  cudaEvent_t ev[kIoEvents] = {};
 };
 
 static void plan_free(gnc_fbp_plan *p) {
@@ -164,6 +172,12 @@ static void plan_free(gnc_fbp_plan *p) {
   cudaFree(p->offset);
   cudaFree(p->tilt_factor);
   cudaFree(p->err);
+  cudaFree(p->io_in);
+  cudaFree(p->io_out);
+  for (cudaEvent_t e : p->ev)
+    if (e) cudaEventDestroy(e);
+  if (p->s_in) cudaStreamDestroy(p->s_in);
+  if (p->s_out) cudaStreamDestroy(p->s_out);
 }
 
 template <typename T>
@@ -401,29 +415,121 @@ int gnc_fbp_execute(gnc_fbp_plan *p, const float *d_input, float *d_volume, void
   return gnc_fbp_backproject(p, d_volume, 0, stream);
 }
 
+// Host buffers in and out, with the copies overlapped with the kernels: the
+// input goes up in tilt groups, each group's transforms start as soon as it
+// has arrived; the backprojection runs in row slabs and each finished slab
+// goes down while the next one is computed.  Device buffers, streams and
+// events are created on the first call and kept with the plan.
+static cudaError_t io_setup(gnc_fbp_plan *p, size_t in_elems, size_t out_elems) {
+  cudaError_t e = cudaSuccess;
+  if (!p->io_in) e = cudaMalloc((void **)&p->io_in, in_elems * sizeof(float));
+  if (e == cudaSuccess && !p->io_out) e = cudaMalloc((void **)&p->io_out, out_elems * sizeof(float));
+  if (e == cudaSuccess && !p->s_in) e = cudaStreamCreateWithFlags(&p->s_in, cudaStreamNonBlocking);
+  if (e == cudaSuccess && !p->s_out) e = cudaStreamCreateWithFlags(&p->s_out, cudaStreamNonBlocking);
+  for (int i = 0; e == cudaSuccess && i < kIoEvents; ++i)
+    if (!p->ev[i]) e = cudaEventCreateWithFlags(&p->ev[i], cudaEventDisableTiming);
+  return e;
+}
+
+static int execute_host_pipelined(gnc_fbp_plan *p, const float *h_input, float *h_volume,
+                                  cudaStream_t s) {
+  const size_t per_tilt = (size_t)(p->input == GNC_INPUT_CORRECTED ? p->D : 1) * p->H * p->W;
+  const size_t plane = (size_t)p->Z * p->X;
+  cudaEvent_t *ev_in = p->ev, *ev_bp = p->ev + kIoGroups;
+  cudaEvent_t ev_start = p->ev[kIoEvents - 2], ev_done = p->ev[kIoEvents - 1];
+  // the previous call's reads of the I/O buffers are ordered before this one
+  GNC_CUDA(cudaEventRecord(ev_start, s));
+  GNC_CUDA(cudaStreamWaitEvent(p->s_in, ev_start, 0));
+  GNC_CUDA(cudaStreamWaitEvent(p->s_out, ev_start, 0));
+  const int group = std::max(8, (p->T + kIoGroups - 1) / kIoGroups);
+  for (int g = 0, t0 = 0; t0 < p->T; ++g, t0 += group) {
+    const int n = std::min(group, p->T - t0);
+    GNC_CUDA(cudaMemcpyAsync(p->io_in + (size_t)t0 * per_tilt, h_input + (size_t)t0 * per_tilt,
+                             n * per_tilt * sizeof(float), cudaMemcpyHostToDevice, p->s_in));
+    GNC_CUDA(cudaEventRecord(ev_in[g], p->s_in));
+  }
+  RowStageArgs r{};
+  r.D = p->D;
+  r.H = p->H;
+  r.N = p->W;
+  r.T = p->T;
+  r.ramp = 1;
+  r.tilt_factor = p->tilt_factor;
+  r.out_staged = 1;
+  r.staging = p->staging;
+  r.staged = p->staged;
+  r.row_exp = p->row_exp;
+  if (p->correct) {
+    GNC_CUDA(launch_sign_table(p->sargs, p->sign, s));
+    r.input_spectra = 1;
+    r.g = p->gbuf;
+  } else {
+    r.input_spectra = 0;
+    r.rows = p->io_in;
+    r.row_stride = p->W;
+    r.plane_stride = (long)p->H * p->W;
+  }
+  const size_t half = p->W / 2;
+  for (int g = 0, t0 = 0; t0 < p->T; ++g, t0 += group) {
+    const int n = std::min(group, p->T - t0);
+    GNC_CUDA(cudaStreamWaitEvent(s, ev_in[g], 0));
+    if (p->correct) {
+      float2 *spec = p->spec + (size_t)t0 * p->H * half;
+      GNC_CUDA(launch_rfft_rows(p->io_in + (size_t)t0 * per_tilt, spec, n, p->H, p->W, s));
+      GNC_CUDA(launch_column_fft(spec, n, p->H, p->W, s));
+      for (int c0 = t0; c0 < t0 + n; c0 += p->chunk) {
+        const int nt = std::min(p->chunk, t0 + n - c0);
+        GNC_CUDA(launch_column_flip(p->spec, p->gbuf, p->sign, c0, nt, p->D, p->H, p->W, s));
+        r.nt = nt;
+        r.t0 = c0;
+        GNC_CUDA(launch_row_stage(r, s));
+      }
+    } else {
+      r.nt = n;
+      r.t0 = t0;
+      GNC_CUDA(launch_row_stage(r, s));
+    }
+  }
+  // backprojection in slabs of whole row pairs, each copied out when done
+  const int rows = ((p->H + 7) / 8 + 7) / 8 * 8;  // at most 8 slabs of whole block rows
+  const size_t pb = p->staging == GNC_STAGE_F16 ? sizeof(__half2) : sizeof(float2);
+  for (int j = 0, y0 = 0; y0 < p->H; ++j, y0 += rows) {
+    const int ny = std::min(rows, p->H - y0);
+    BpArgs a = bp_args(p, p->io_out + (size_t)y0 * plane);
+    const size_t pair0 = (size_t)(y0 / 2) * p->D * p->T;
+    a.Y = ny;
+    a.staged = (const unsigned char *)p->staged + pair0 * p->W * pb;
+    a.row_exp = p->row_exp ? p->row_exp + 2 * pair0 : nullptr;
+    a.offset = p->offset + (size_t)y0 * p->T;
+    if (!p->uniform_centre)
+      GNC_CUDA(launch_backproject_exact(a, s));
+    else
+      GNC_CUDA(launch_backproject_fast(a, s));
+    GNC_CUDA(cudaEventRecord(ev_bp[j], s));
+    GNC_CUDA(cudaStreamWaitEvent(p->s_out, ev_bp[j], 0));
+    GNC_CUDA(cudaMemcpyAsync(h_volume + (size_t)y0 * plane, p->io_out + (size_t)y0 * plane,
+                             ny * plane * sizeof(float), cudaMemcpyDeviceToHost, p->s_out));
+  }
+  GNC_CUDA(cudaEventRecord(ev_done, p->s_out));
+  GNC_CUDA(cudaStreamWaitEvent(s, ev_done, 0));
+  return GNC_OK;
+}
+
 int gnc_fbp_execute_host(gnc_fbp_plan *p, const float *h_input, float *h_volume, void *stream) {
   GNC_REQUIRE(p != nullptr && h_input != nullptr && h_volume != nullptr);
   cudaStream_t s = (cudaStream_t)stream;
   size_t in_elems = (size_t)p->T * (p->input == GNC_INPUT_CORRECTED ? p->D : 1) * p->H * p->W;
   size_t out_elems = (size_t)p->H * p->Z * p->X;
-  float *din = nullptr, *dout = nullptr;
-  GNC_CUDA(cudaMallocAsync((void **)&din, in_elems * sizeof(float), s));
-  cudaError_t e = cudaMallocAsync((void **)&dout, out_elems * sizeof(float), s);
-  if (e != cudaSuccess) {
-    cudaFreeAsync(din, s);
-    GNC_CUDA(e);
-  }
-  int st = GNC_OK;
-  e = cudaMemcpyAsync(din, h_input, in_elems * sizeof(float), cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) st = gnc_fbp_execute(p, din, dout, stream);
-  if (e == cudaSuccess && st == GNC_OK)
-    e = cudaMemcpyAsync(h_volume, dout, out_elems * sizeof(float), cudaMemcpyDeviceToHost, s);
-  cudaFreeAsync(din, s);
-  cudaFreeAsync(dout, s);
-  cudaError_t e2 = cudaStreamSynchronize(s);
+  GNC_CUDA(io_setup(p, in_elems, out_elems));
+  int st = execute_host_pipelined(p, h_input, h_volume, s);
+  // whatever was queued finishes before the host buffers go back to the caller
+  cudaError_t e1 = cudaStreamSynchronize(p->s_in);
+  cudaError_t e2 = cudaStreamSynchronize(p->s_out);
+  cudaError_t e3 = cudaStreamSynchronize(s);
   if (st != GNC_OK) return st;
-  GNC_CUDA(e);
+  GNC_CUDA(e1);
   GNC_CUDA(e2);
+  GNC_CUDA(e3);
   return GNC_OK;
 }
 

@@ -196,8 +196,12 @@ GNC_API size_t gnc_fbp_workspace_bytes(const gnc_fbp_plan *plan);
  * device, overwritten. */
 GNC_API int gnc_fbp_execute(gnc_fbp_plan *plan, const float *d_input, float *d_volume,
                             void *stream);
-/* The same from host buffers: copies in, executes, copies out, synchronises
- * the stream.  Pinned host memory gives the fastest copies. */
+/* The same from host buffers, synchronising before it returns.  The input
+ * goes up in tilt groups and the volume comes down in row slabs, overlapped
+ * with the kernels on two streams of the plan; the first call creates them
+ * and the device input/output buffers (kept until the plan is destroyed, not
+ * counted by gnc_fbp_workspace_bytes).  Pinned host memory gives the fastest
+ * copies. */
 GNC_API int gnc_fbp_execute_host(gnc_fbp_plan *plan, const float *h_input, float *h_volume,
                                  void *stream);
 /* Correction only: raw (T, H, W) -> corrected stack (T, D, H, W), the output

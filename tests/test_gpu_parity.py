@@ -224,6 +224,24 @@ def test_pipeline_vs_oracles(torch, oracle, staging, shape):
         assert rel_l2(vol, ref64) < FP16_TOL
 
 
+# The host-buffer entry point overlaps its copies with the kernels (tilt groups
+# in, row slabs out); it must give exactly the device entry point's volume.
+@pytest.mark.parametrize("staging", ["f32", "f16"])
+@pytest.mark.parametrize("T,H,W,Z,D,ragged", [(37, 64, 256, 40, 4, False), (19, 90, 128, 30, 3, True),
+                                                (9, 22, 64, 48, 1, False)])
+def test_host_pipeline_equals_device_path(torch, oracle, staging, T, H, W, Z, D, ragged):
+    centre = None
+    if ragged:  # per-row centres: the exact backprojector
+        centre = (W / 2 + 0.25 * np.sin(np.arange(H))).astype(np.float32)
+    plan, proj, *_ = _plan_case(oracle, T=T, H=H, W=W, Z=Z, D=D, staging=staging, centre=centre)
+    want = torch.empty(plan.volume_shape, dtype=torch.float32, device="cuda")
+    plan.execute(dev(torch, proj), want)
+    torch.cuda.synchronize()
+    for _ in range(2):  # the second call reuses the plan's I/O buffers and streams
+        got = plan.execute_host(proj)
+        np.testing.assert_array_equal(got, want.cpu().numpy())
+
+
 def test_pipeline_exact_backprojector_equals_fast(torch, oracle):
     plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=15, H=10, W=64, Z=48, D=6)
     inp = dev(torch, proj)
