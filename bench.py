@@ -215,6 +215,7 @@ def run_ours(args, rank, world, dist):
     value16 = units / (total16 * 1e-3) / 1e9
     e2e_value = units / (e2e_ms * 1e-3) / 1e9
 
+    serving = run_serving(dev) if not args.no_serve else None
     parity = cpu = None
     if rank == 0 and not args.no_cpu:
         parity, cpu = oracle_sample(proj, vols)
@@ -284,11 +285,141 @@ def run_ours(args, rank, world, dist):
         # kernels of this library launched in the timed region of `value`
         "gpu_launches": int(p32.launches_per_execute * args.steps),
     }
+    if serving is not None:
+        line["serving"] = serving
     if cpu is not None:
         line["cpu_baseline"] = cpu
     if parity is not None:
         line["parity"] = parity
     print(json.dumps(line))
+
+
+# ------------------------------------------------------------------ serving
+SERVE = dict(requests=2000, seed=5, budget_gb=96, slots=8, load=0.8, burst=48)
+SERVE_NAME = ("serving stream: Poisson arrivals, projections 128^2..512^2, 31/41/61 tilts over "
+              "+-60 deg, df U[10000, 50000] A, ndf U{1..10}, thickness size/2, FP16/FP32 mixed")
+
+
+def serving_inputs(dev):
+    """One seeded blob-phantom tilt series per (size, tilts), page-locked."""
+    from guanaco_gb300 import serve, synthetic
+
+    inputs = {}
+    for n in (128, 256, 384, 512):
+        blobs = synthetic.blob_phantom(max(64, n), n, n, n // 2, seed=n)
+        for T in (31, 41, 61):
+            ang = np.deg2rad(np.linspace(-60, 60, T)).astype(np.float32)
+            t = synthetic.tilt_series(blobs, ang, n, n, defocus=30000.0, noise=0.1, seed=n + T,
+                                      device=dev)
+            h = serve.pinned_empty((T, n, n))
+            h[...] = t.cpu().numpy()
+            inputs[(n, T)] = h
+    return inputs
+
+
+def serving_desc(r):
+    import guanaco_gb300 as G
+
+    n, T = r["size"], r["tilts"]
+    ang = np.deg2rad(np.linspace(-60, 60, T)).astype(np.float32)
+    c = G.get_centre((T, n, n), None, False)
+    mn, mx, step, nd = G.get_defocus_steps(r["defocus"], r["ndf"], None, n, c, 1.0)
+    return G.FbpDesc(T, n, n, ang, grid_height=r["thickness"], grid_width=n, centre=c,
+                     pixel_size=1.0, input="raw", correct=True, num_defocus=nd,
+                     slab_defocus=G.api.slab_defoci(mn, nd, step),
+                     min_defocus=float(mn - r["defocus"]), max_defocus=float(mx - r["defocus"]),
+                     energy=300.0, spherical_aberration=2.7, staging=r["staging"])
+
+
+def drive_stream(srv, stream, descs, inputs, pools, t_base):
+    """Submits each request at its arrival time (server clock t_base + arrival);
+    returns per-request (latency s, voxel-tilts, info).  A request whose output
+    pool is empty waits for the oldest one of its size (client back-pressure);
+    its latency still counts from the scheduled arrival."""
+    outstanding = {}
+    done = []
+
+    def finish(rid, info):
+        r, buf = outstanding.pop(rid)
+        pools[r["size"]].append(buf)
+        done.append((info["t_done"] - (t_base + r["arrival"]), descs[r["id"]].voxel_tilts, info))
+
+    def reap():
+        for rid in list(outstanding):
+            info = srv.wait(rid, timeout=0.0)
+            if info is not None:
+                finish(rid, info)
+
+    for r in stream:
+        target = t_base + r["arrival"]
+        while True:
+            reap()
+            now = srv.now()
+            if now >= target:
+                break
+            time.sleep(min(target - now, 2e-4))
+        while not pools[r["size"]]:
+            rid = min((k for k, v in outstanding.items() if v[0]["size"] == r["size"]))
+            finish(rid, srv.wait(rid))
+        buf = pools[r["size"]].pop()
+        rid = srv.submit(descs[r["id"]], inputs[(r["size"], r["tilts"])], buf)
+        outstanding[rid] = (r, buf)
+    for rid in list(outstanding):
+        finish(rid, srv.wait(rid))
+    return done
+
+
+def run_serving(dev):
+    """The mixed serving stream through the request server: a burst of
+    SERVE['burst'] requests measures the capacity (and warms the plan cache),
+    then SERVE['requests'] Poisson arrivals at SERVE['load'] of it."""
+    from guanaco_gb300 import serve, synthetic
+
+    inputs = serving_inputs(dev)
+    cfg = SERVE
+    pools = {n: [serve.pinned_empty((n, n // 2, n)) for _ in range(cfg["slots"] + 8)]
+             for n in (128, 256, 384, 512)}
+    with serve.Server(budget_bytes=cfg["budget_gb"] << 30, slots=cfg["slots"]) as srv:
+        burst = synthetic.request_stream(cfg["burst"], 1e9, seed=cfg["seed"] + 1)
+        bdesc = [serving_desc(r) for r in burst]
+        t0 = srv.now() + 0.01
+        res = drive_stream(srv, burst, bdesc, inputs, pools, t0)
+        span = max(i["t_done"] for _, _, i in res) - t0
+        capacity = len(burst) / span
+        rate = cfg["load"] * capacity
+        stream = synthetic.request_stream(cfg["requests"], rate, seed=cfg["seed"])
+        descs = [serving_desc(r) for r in stream]
+        t_base = srv.now() + 0.05
+        res = drive_stream(srv, stream, descs, inputs, pools, t_base)
+        stats = srv.stats()
+    lat = np.array([x[0] for x in res]) * 1e3
+    span = max(x[2]["t_done"] for x in res) - t_base
+    vt = sum(x[1] for x in res)
+    return {
+        "workload": SERVE_NAME,
+        "requests": len(res),
+        "p50_ms": round(float(np.percentile(lat, 50)), 3),
+        "p99_ms": round(float(np.percentile(lat, 99)), 3),
+        "max_ms": round(float(lat.max()), 3),
+        "mean_ms": round(float(lat.mean()), 3),
+        "throughput_req_s": round(len(res) / span, 1),
+        "value": round(vt / span / 1e9, 2),
+        "unit": UNIT,
+        "rate_hz": round(rate, 1),
+        "load": cfg["load"],
+        "burst_capacity_req_s": round(capacity, 1),
+        "slots": cfg["slots"],
+        "budget_gb": cfg["budget_gb"],
+        "graph_replays": int(stats["graph_launches"]),
+        "direct_runs": int(stats["direct_launches"]),
+        "plans_created": int(stats["plans_created"]),
+        "plans_evicted": int(stats["plans_evicted"]),
+        "peak_in_flight": int(stats["peak_in_flight"]),
+        "failed": int(stats["failed"]),
+        "inputs": ("one seeded blob-phantom series per (size, tilts), reused with each "
+                   "request's own defocus, ndf and staging; latency from the scheduled arrival "
+                   "to the volume in page-locked host memory"),
+    }
 
 
 def oracle_sample(proj, vols, nrows=8):
@@ -409,6 +540,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the oracle parity/CPU sample")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving stream")
     ap.add_argument("--case", choices=["3dctf", "profile"], default="3dctf",
                     help="profile: the same 1024^2 ndf=10 kernels on 16 tilts and a 64-voxel-"
                          "thick volume, small enough for ncu captures (not a bench line)")
@@ -416,6 +548,7 @@ def main():
     if args.case == "profile":
         global WORKLOAD_NAME
         WL.update(T=16, Z=64, blobs=200)
+        args.no_serve = True
         WORKLOAD_NAME = "profiling case: " + WORKLOAD_NAME.replace("61 tilts", "16 tilts").replace(
             "x300", "x64")
         args.no_cpu = True

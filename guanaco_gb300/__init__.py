@@ -7,6 +7,8 @@
   ``guanaco`` functions on the device path; ``reconstruct_ctf`` runs both in
   one device pass.
 * ``FbpPlan`` -- the whole-series plan over the C ABI (include/guanaco_gb300.h).
+* ``serve.Server`` -- the request server: many tilt series of mixed shapes at
+  once, with continuous batching on one GPU.
 """
 from . import detail  # noqa: F401
 from .api import (  # noqa: F401
@@ -20,6 +22,6 @@ from .api import (  # noqa: F401
     reconstruct,
     reconstruct_ctf,
 )
-from .fbp import FbpPlan  # noqa: F401
+from .fbp import FbpDesc, FbpPlan  # noqa: F401
 
 __version__ = "0.1.0"

@@ -18,6 +18,7 @@ GNC_ERR_UNSUPPORTED = 2
 GNC_ERR_CUDA = 3
 GNC_ERR_OUT_OF_MEMORY = 4
 GNC_ERR_DEVICE = 5
+GNC_ERR_PENDING = 6
 
 GNC_STAGE_F32 = 0
 GNC_STAGE_F16 = 1
@@ -86,6 +87,24 @@ class GncFbpDesc(ctypes.Structure):
     ]
 
 
+class GncRequestInfo(ctypes.Structure):
+    """gnc_request_info: outcome and server-clock times of one served request."""
+
+    _fields_ = [("status", c_int), ("graph", c_int), ("device_error", c_int),
+                ("t_submit", c_double), ("t_start", c_double), ("t_done", c_double)]
+
+
+class GncServerStats(ctypes.Structure):
+    """gnc_server_stats."""
+
+    _fields_ = [(n, ctypes.c_uint64) for n in ("submitted", "completed", "failed", "graph_launches",
+                                                "direct_launches", "plans_created",
+                                                "plans_evicted")] + \
+               [("budget_bytes", c_size), ("bytes_in_use", c_size)] + \
+               [(n, c_int) for n in ("slots", "cached_plans", "in_flight", "peak_in_flight",
+                                     "queued")]
+
+
 # Every symbol include/guanaco_gb300.h declares, with (restype, argtypes).
 SIGNATURES = {
     "gnc_last_error": (ctypes.c_char_p, []),
@@ -120,6 +139,14 @@ SIGNATURES = {
     "gnc_fbp_staged": (c_int, [c_void, ctypes.POINTER(c_void), ctypes.POINTER(c_void)]),
     "gnc_fbp_check": (c_int, [c_void, c_void]),
     "gnc_fbp_launches": (c_int, [c_void]),
+    "gnc_server_create": (c_int, [c_size, c_int, ctypes.POINTER(c_void)]),
+    "gnc_server_destroy": (c_int, [c_void]),
+    "gnc_server_submit": (c_int, [c_void, ctypes.POINTER(GncFbpDesc), c_void, c_void,
+                                  ctypes.POINTER(ctypes.c_uint64)]),
+    "gnc_server_wait": (c_int, [c_void, ctypes.c_uint64, c_double,
+                                ctypes.POINTER(GncRequestInfo)]),
+    "gnc_server_now": (c_double, [c_void]),
+    "gnc_server_get_stats": (c_int, [c_void, ctypes.POINTER(GncServerStats)]),
 }
 
 

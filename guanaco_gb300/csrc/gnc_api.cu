@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <map>
 #include <mutex>
 #include <string>
@@ -16,6 +17,7 @@
 
 #include "../../include/guanaco_gb300.h"
 #include "gnc_common.cuh"
+#include "gnc_plan_hooks.h"
 
 namespace gnc {
 
@@ -135,6 +137,31 @@ using namespace gnc;
 // copies out in up to kIoSlabs row slabs, plus two events for the stream joins.
 constexpr int kIoGroups = 32, kIoSlabs = 8, kIoEvents = kIoGroups + kIoSlabs + 2;
 
+// Per-request parameter block of a plan: the same byte layout on the host and
+// on the device, so one copy moves all of it.
+struct ParamLayout {
+  size_t sign, bp, geom, factor, slab, offset, bytes;
+};
+static ParamLayout param_layout(int T, int H, int D) {
+  auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  ParamLayout L{};
+  size_t o = 0;
+  L.sign = o;
+  o = up(o + sizeof(SignTableArgs));
+  L.bp = o;
+  o = up(o + 2 * sizeof(float));
+  L.geom = o;
+  o = up(o + (size_t)T * sizeof(TiltGeom));
+  L.factor = o;
+  o = up(o + (size_t)T * sizeof(float));
+  L.slab = o;
+  o = up(o + (size_t)D * sizeof(double));
+  L.offset = o;
+  o = up(o + (size_t)H * T * sizeof(float));
+  L.bytes = o;
+  return L;
+}
+
 struct gnc_fbp_plan {
   int device = 0;
   int T = 0, H = 0, W = 0, Z = 0, X = 0, D = 1, Y2 = 0;
@@ -149,6 +176,12 @@ struct gnc_fbp_plan {
   void *staged = nullptr;   // (Y2, D, T, W) pairs
   int8_t *row_exp = nullptr;
   int8_t *sign = nullptr;   // (D, H, W/2 + 1)
+  // everything that differs between two requests of the same shape, in one
+  // block (ParamLayout): views into it
+  unsigned char *params = nullptr;
+  ParamLayout pl{};
+  SignTableArgs *dyn_sign = nullptr;
+  float *dyn_bp = nullptr;  // (dscale, doffset)
   double *slab_df = nullptr;
   TiltGeom *geom = nullptr;
   float *offset = nullptr;  // (H, T)
@@ -167,10 +200,7 @@ static void plan_free(gnc_fbp_plan *p) {
   cudaFree(p->staged);
   cudaFree(p->row_exp);
   cudaFree(p->sign);
-  cudaFree(p->slab_df);
-  cudaFree(p->geom);
-  cudaFree(p->offset);
-  cudaFree(p->tilt_factor);
+  cudaFree(p->params);
   cudaFree(p->err);
   cudaFree(p->io_in);
   cudaFree(p->io_out);
@@ -205,17 +235,63 @@ static BpArgs bp_args(const gnc_fbp_plan *p, float *vol) {
   a.uniform_centre = p->uniform_centre ? 1 : 0;
   a.vol = vol;
   a.err = p->err;
+  a.dyn = p->dyn_bp;
   return a;
 }
 
-extern "C" {
+// Fills the parameter block `blk` (layout p->pl) for descriptor d: the tilt
+// geometry and per-row detector offsets (reconstructor.cpp:35-47), per-tilt
+// factors (weight and sign, mp.py:128-141), slab defoci, the CTF arguments of
+// the sign table and the slab map (dscale, doffset).  Also returns whether all
+// rows share one centre and the host copies of the by-value arguments.
+static void fill_params(const gnc_fbp_plan *p, const gnc_fbp_desc *d, unsigned char *blk,
+                        bool *uniform, float *dscale, float *doffset, SignTableArgs *sargs) {
+  const ParamLayout &L = p->pl;
+  const float min_def = d->num_defocus > 1 ? d->min_defocus : 0.f;
+  const float max_def = d->num_defocus > 1 ? d->max_defocus : 0.f;
+  defocus_scale(d->num_defocus, d->pixel_size, min_def, max_def, dscale, doffset);
+  float *bp = (float *)(blk + L.bp);
+  bp[0] = *dscale;
+  bp[1] = *doffset;
+  TiltGeom *geom = (TiltGeom *)(blk + L.geom);
+  float *offset = (float *)(blk + L.offset);
+  std::vector<float> centre(p->H);
+  for (int y = 0; y < p->H; ++y) centre[y] = d->centre ? d->centre[y] : (float)(p->W * 0.5);
+  *uniform = true;
+  for (int y = 1; y < p->H; ++y)
+    if (centre[y] != centre[0]) *uniform = false;
+  for (int y = 0; y < p->H; ++y)
+    for (int t = 0; t < p->T; ++t)
+      geom[t] = tilt_geometry(d->angles[t], centre[y], d->num_angles, &offset[(size_t)y * p->T + t]);
+  float *factor = (float *)(blk + L.factor);
+  for (int t = 0; t < p->T; ++t)
+    factor[t] = (float)((d->minus ? -1.0 : 1.0) * (d->weights ? d->weights[t] : 1.0));
+  double *slab = (double *)(blk + L.slab);
+  SignTableArgs sa{};
+  if (p->correct) {
+    for (int k = 0; k < p->D; ++k) slab[k] = d->slab_defocus[k];
+    sa.D = p->D;
+    sa.H = p->H;
+    sa.W = p->W;
+    sa.inv_ps = 1.0 / (d->ctf_pixel_size > 0 ? d->ctf_pixel_size : (double)d->pixel_size);
+    sa.l = gnc_get_electron_wavelength(d->energy_kev * 1000);
+    sa.Cs = d->cs_mm * 1e7;
+    sa.Ca = d->astigmatism;
+    sa.Pa = d->astigmatism_angle_deg * M_PI / 180;
+    sa.phi = d->phase_shift_deg * M_PI / 180;
+    sa.slab_df = p->slab_df;
+    fill_sign_screen(&sa);
+  }
+  std::memcpy(blk + L.sign, &sa, sizeof(sa));  // the device copy has dyn = null
+  sa.dyn = p->dyn_sign;
+  *sargs = sa;
+}
 
-const char *gnc_last_error(void) { return last_error(); }
-int gnc_version(void) { return 100; }
+// ------------------------------------------- hooks for the request server --
+namespace gnc {
 
-int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
-  GNC_REQUIRE(d != nullptr && out != nullptr);
-  *out = nullptr;
+int desc_check(const gnc_fbp_desc *d) {
+  GNC_REQUIRE(d != nullptr);
   GNC_REQUIRE(d->num_angles > 0);
   GNC_REQUIRE(d->height > 0);
   GNC_REQUIRE(d->width > 0);
@@ -239,6 +315,84 @@ int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
               "height <= 8192 that also factorise)");
     return GNC_ERR_UNSUPPORTED;
   }
+  return GNC_OK;
+}
+
+// Device bytes gnc_fbp_plan_create allocates for d (the same sizes, without
+// allocating), plus the input and output buffers of one request.
+size_t plan_bytes(const gnc_fbp_desc *d) {
+  const size_t T = d->num_angles, H = d->height, W = d->width, D = d->num_defocus;
+  const size_t Y2 = (H + 1) / 2, half = W / 2;
+  const bool ctf = d->input == GNC_INPUT_RAW && d->correct;
+  size_t b = param_layout((int)T, (int)H, (int)D).bytes + sizeof(int);
+  if (ctf) {
+    const size_t per_tilt = D * H * half * sizeof(float2);
+    const size_t chunk = std::max<size_t>(1, std::min<size_t>(T, (48ull << 20) / per_tilt));
+    b += T * H * half * sizeof(float2) + chunk * D * H * half * sizeof(float2) + D * H * (half + 1);
+  }
+  const size_t pb = d->staging == GNC_STAGE_F16 ? sizeof(__half2) : sizeof(float2);
+  b += (Y2 * D * T * W + 8) * pb;
+  if (d->staging == GNC_STAGE_F16) b += Y2 * D * T * 2;
+  const size_t in_elems = T * (d->input == GNC_INPUT_CORRECTED ? D : 1) * H * W;
+  b += (in_elems + H * d->grid_height * d->grid_width) * sizeof(float);
+  return b;
+}
+
+// Everything that fixes a plan's buffers and its sequence of launches; two
+// requests with the same key can share one plan and one captured graph.
+std::string plan_key(const gnc_fbp_desc *d) {
+  float dscale, doffset;
+  const float mn = d->num_defocus > 1 ? d->min_defocus : 0.f;
+  const float mx = d->num_defocus > 1 ? d->max_defocus : 0.f;
+  defocus_scale(d->num_defocus, d->pixel_size, mn, mx, &dscale, &doffset);
+  bool uniform = true;
+  if (d->centre)
+    for (size_t y = 1; y < d->height; ++y)
+      if (d->centre[y] != d->centre[0]) uniform = false;
+  BpArgs a{};
+  a.staging = d->staging;
+  a.N = (int)d->width;
+  a.D = (int)d->num_defocus;
+  a.dscale = dscale;
+  a.uniform_centre = uniform ? 1 : 0;
+  char buf[256];
+  snprintf(buf, sizeof buf, "%zu,%zu,%zu,%zu,%zu,%zu,%d,%d,%d,%d", d->num_angles, d->height,
+           d->width, d->grid_height, d->grid_width, d->num_defocus, d->input,
+           (d->input == GNC_INPUT_RAW && d->correct) ? 1 : 0, d->staging,
+           backproject_fast_variant(a));
+  return buf;
+}
+
+size_t plan_param_bytes(const gnc_fbp_plan *p) { return p->pl.bytes; }
+
+// Points the plan at a new request of the same key: fills the parameter block
+// in `host_block` (page-locked, plan_param_bytes long, not in use by an
+// earlier copy) and enqueues its copy to the device on s.
+int plan_set_request(gnc_fbp_plan *p, const gnc_fbp_desc *d, unsigned char *host_block,
+                     cudaStream_t s) {
+  bool uniform;
+  std::memset(host_block, 0, p->pl.bytes);
+  fill_params(p, d, host_block, &uniform, &p->dscale, &p->doffset, &p->sargs);
+  GNC_REQUIRE(uniform == p->uniform_centre);
+  GNC_CUDA(cudaMemcpyAsync(p->params, host_block, p->pl.bytes, cudaMemcpyHostToDevice, s));
+  return GNC_OK;
+}
+
+int *plan_error_word(gnc_fbp_plan *p) { return p->err; }
+
+}  // namespace gnc
+
+extern "C" {
+
+const char *gnc_last_error(void) { return last_error(); }
+int gnc_version(void) { return 100; }
+
+int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
+  GNC_REQUIRE(d != nullptr && out != nullptr);
+  *out = nullptr;
+  const int st = gnc::desc_check(d);
+  if (st != GNC_OK) return st;
+  const bool ctf = d->input == GNC_INPUT_RAW && d->correct;
   auto *p = new gnc_fbp_plan();
   cudaGetDevice(&p->device);
   p->T = (int)d->num_angles;
@@ -254,47 +408,28 @@ int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
   p->pixel_size = d->pixel_size;
   p->min_def = d->num_defocus > 1 ? d->min_defocus : 0.f;
   p->max_def = d->num_defocus > 1 ? d->max_defocus : 0.f;
-  defocus_scale(d->num_defocus, d->pixel_size, p->min_def, p->max_def, &p->dscale, &p->doffset);
-
-  // geometry tables
-  std::vector<TiltGeom> geom(p->T);
-  std::vector<float> offset((size_t)p->H * p->T);
-  std::vector<float> centre(p->H);
-  for (int y = 0; y < p->H; ++y) centre[y] = d->centre ? d->centre[y] : (float)(p->W * 0.5);
-  for (int y = 1; y < p->H; ++y)
-    if (centre[y] != centre[0]) p->uniform_centre = false;
-  for (int y = 0; y < p->H; ++y)
-    for (int t = 0; t < p->T; ++t)
-      geom[t] = tilt_geometry(d->angles[t], centre[y], d->num_angles, &offset[(size_t)y * p->T + t]);
-  std::vector<float> factor;
-  if (d->weights || d->minus) {
-    factor.resize(p->T);
-    for (int t = 0; t < p->T; ++t)
-      factor[t] = (float)((d->minus ? -1.0 : 1.0) * (d->weights ? d->weights[t] : 1.0));
-  }
 
   const size_t half = (size_t)p->W / 2;
   cudaError_t e = cudaSuccess;
+  p->pl = param_layout(p->T, p->H, p->D);
+  e = dalloc(p, &p->params, p->pl.bytes);
+  if (e == cudaSuccess) {
+    p->dyn_sign = (SignTableArgs *)(p->params + p->pl.sign);
+    p->dyn_bp = (float *)(p->params + p->pl.bp);
+    p->geom = (TiltGeom *)(p->params + p->pl.geom);
+    p->tilt_factor = (float *)(p->params + p->pl.factor);
+    p->slab_df = (double *)(p->params + p->pl.slab);
+    p->offset = (float *)(p->params + p->pl.offset);
+    std::vector<unsigned char> blk(p->pl.bytes, 0);
+    fill_params(p, d, blk.data(), &p->uniform_centre, &p->dscale, &p->doffset, &p->sargs);
+    e = cudaMemcpy(p->params, blk.data(), blk.size(), cudaMemcpyHostToDevice);
+  }
   if (ctf) {
     size_t per_tilt = (size_t)p->D * p->H * half * sizeof(float2);
     p->chunk = (int)std::max<size_t>(1, std::min<size_t>(p->T, (48ull << 20) / per_tilt));
     if (e == cudaSuccess) e = dalloc(p, &p->spec, (size_t)p->T * p->H * half);
     if (e == cudaSuccess) e = dalloc(p, &p->gbuf, (size_t)p->chunk * p->D * p->H * half);
     if (e == cudaSuccess) e = dalloc(p, &p->sign, (size_t)p->D * p->H * (half + 1));
-    if (e == cudaSuccess) e = dalloc(p, &p->slab_df, (size_t)p->D);
-    if (e == cudaSuccess)
-      e = cudaMemcpy(p->slab_df, d->slab_defocus, p->D * sizeof(double), cudaMemcpyHostToDevice);
-    p->sargs.D = p->D;
-    p->sargs.H = p->H;
-    p->sargs.W = p->W;
-    p->sargs.inv_ps = 1.0 / (d->ctf_pixel_size > 0 ? d->ctf_pixel_size : (double)d->pixel_size);
-    p->sargs.l = gnc_get_electron_wavelength(d->energy_kev * 1000);
-    p->sargs.Cs = d->cs_mm * 1e7;
-    p->sargs.Ca = d->astigmatism;
-    p->sargs.Pa = d->astigmatism_angle_deg * M_PI / 180;
-    p->sargs.phi = d->phase_shift_deg * M_PI / 180;
-    p->sargs.slab_df = p->slab_df;
-    fill_sign_screen(&p->sargs);
   }
   // +8 pixels: a 16-byte aligned bulk copy of the last row may run past its end
   const size_t elems = (size_t)p->Y2 * p->D * p->T * p->W + 8;
@@ -305,18 +440,6 @@ int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
     e = dalloc(p, &p->row_exp, (size_t)p->Y2 * p->D * p->T * 2);
   if (e == cudaSuccess) e = dalloc(p, &p->err, 1);
   if (e == cudaSuccess) e = cudaMemset(p->err, 0, sizeof(int));
-  if (e == cudaSuccess) e = dalloc(p, &p->geom, (size_t)p->T);
-  if (e == cudaSuccess) e = dalloc(p, &p->offset, offset.size());
-  if (e == cudaSuccess)
-    e = cudaMemcpy(p->geom, geom.data(), geom.size() * sizeof(TiltGeom), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess)
-    e = cudaMemcpy(p->offset, offset.data(), offset.size() * sizeof(float), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess && !factor.empty()) {
-    e = dalloc(p, &p->tilt_factor, factor.size());
-    if (e == cudaSuccess)
-      e = cudaMemcpy(p->tilt_factor, factor.data(), factor.size() * sizeof(float),
-                     cudaMemcpyHostToDevice);
-  }
   if (e != cudaSuccess) {
     set_error(std::string("gnc_fbp_plan_create: ") + cudaGetErrorString(e));
     plan_free(p);

@@ -20,6 +20,10 @@ __device__ __forceinline__ float voxel_coord(int i, int n) {
 
 template <bool F16>
 __global__ void k_bp_exact(BpArgs a) {
+  if (a.dyn) {
+    a.dscale = a.dyn[0];
+    a.doffset = a.dyn[1];
+  }
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int z = blockIdx.y * blockDim.y + threadIdx.y;
   const int y2 = blockIdx.z;
@@ -83,6 +87,10 @@ cudaError_t launch_backproject_exact(const BpArgs &a, cudaStream_t s) {
 }
 
 __global__ void k_slab_map(BpArgs a, int32_t *__restrict__ out) {
+  if (a.dyn) {
+    a.dscale = a.dyn[0];
+    a.doffset = a.dyn[1];
+  }
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int z = blockIdx.y * blockDim.y + threadIdx.y;
   const int t = blockIdx.z;

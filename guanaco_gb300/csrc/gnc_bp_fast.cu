@@ -156,6 +156,10 @@ template <int RP, int KMAX, int G, bool F16>
 __global__ void __launch_bounds__(256, 2)
 k_bp_fast(BpArgs a) {
   using P = FastBp<RP, KMAX, G, F16>;
+  if (a.dyn) {
+    a.dscale = a.dyn[0];
+    a.doffset = a.dyn[1];
+  }
   constexpr int A = P::A, B = P::B;
   constexpr int TCH = 128;  // tilts whose parameters are held at once
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -459,6 +463,12 @@ bool backproject_fast_supported(const BpArgs &a) {
   const int align_px = a.staging == kStageF16 ? 4 : 2;
   return a.uniform_centre && a.N % align_px == 0 && max_slabs_per_tile(a, P::TX, P::TZ) <= 4 &&
          a.N >= 2;
+}
+
+int backproject_fast_variant(const BpArgs &a) {
+  using P = FastBp<4, 2, 8, false>;
+  if (!backproject_fast_supported(a)) return 0;
+  return max_slabs_per_tile(a, P::TX, P::TZ) <= 2 ? 2 : 4;
 }
 
 cudaError_t launch_backproject_fast(const BpArgs &a, cudaStream_t s) {

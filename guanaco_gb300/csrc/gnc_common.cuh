@@ -61,6 +61,9 @@ struct SignTableArgs {
   double l, Cs, Ca, Pa, phi;
   const double *slab_df;  // device, D
   float f_a4, f_phipi, f_c2p, f_s2p, f_ips2, f_lca;
+  // device copy of these arguments, or null: when set the kernel reads its
+  // arguments there (a captured launch then serves every request of a plan)
+  const SignTableArgs *dyn;
 };
 void fill_sign_screen(SignTableArgs *a);
 cudaError_t launch_sign_table(const SignTableArgs &a, int8_t *out, cudaStream_t s);
@@ -106,10 +109,14 @@ struct BpArgs {
   int uniform_centre;     // all rows share one centre
   float *vol;             // (Y, Z, X)
   int *err;               // device error word (bounded waits that gave up), or null
+  const float *dyn;       // device (dscale, doffset) overriding the two above, or null
 };
 // The fast kernel's requirements (shared centre, 16-byte aligned rows, at most
 // four slabs per tile); launch_backproject_fast falls back to the exact kernel.
 bool backproject_fast_supported(const BpArgs &a);
+// Which backprojection kernel a launch with these arguments uses: 0 the exact
+// kernel, else the fast kernel's slab capacity per tile (2 or 4).
+int backproject_fast_variant(const BpArgs &a);
 cudaError_t launch_backproject_exact(const BpArgs &a, cudaStream_t s);
 cudaError_t launch_backproject_fast(const BpArgs &a, cudaStream_t s);
 cudaError_t launch_slab_map(const BpArgs &a, int32_t *out, cudaStream_t s);

@@ -74,7 +74,8 @@ __host__ __device__ inline int screened_sign(const SignTableArgs &p, float ldf, 
 }
 
 // One block per (slab, ky) row of the table at a time.
-__global__ void k_sign_table(SignTableArgs a, int8_t *__restrict__ out) {
+__global__ void k_sign_table(SignTableArgs a0, int8_t *__restrict__ out) {
+  const SignTableArgs a = a0.dyn ? *a0.dyn : a0;
   const int sw = a.W / 2 + 1;
   const long rows = (long)a.D * a.H;
   for (long row = blockIdx.x; row < rows; row += gridDim.x) {

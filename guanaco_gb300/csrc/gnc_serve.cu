@@ -1,0 +1,519 @@
+// Request server: continuous batching of whole-series FBP requests on one GPU.
+//
+// One scheduler thread owns the device work.  Callers queue requests
+// (gnc_server_submit); the scheduler admits a request when a slot (a CUDA
+// stream) is free and its plan fits in the device-memory budget, and enqueues
+// on that slot: the parameter upload, the input copy, the device work and the
+// volume copy, followed by a host callback that marks the slot finished.
+// Requests on different slots overlap on the device.
+//
+// Plans are cached by shape (plan_key).  The first request of a shape runs as
+// direct launches, which also creates the FFT tables and kernel attributes the
+// launches need; the same launch sequence is then captured once as a CUDA
+// graph, and later requests of that shape replay it after uploading their own
+// parameter block (the kernels read per-request values from device memory).
+//
+// Admission takes the oldest queued request that can run now; when it cannot
+// (no idle plan of its shape and not enough memory even after releasing idle
+// plans), up to kLookAhead younger requests may pass it, at most kMaxSkips
+// times in a row, after which the scheduler waits for memory to free up.
+//
+// Locking: gn_server::mu guards the queue, the request table, the slots'
+// state, the cache bookkeeping and the statistics.  No CUDA call is made while
+// it is held (a host callback waiting for it would otherwise hold up a device
+// synchronisation inside the CUDA call).
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "gnc_common.cuh"
+#include "gnc_plan_hooks.h"
+
+namespace {
+
+constexpr int kLookAhead = 16;
+constexpr int kMaxSkips = 32;
+
+struct Cached {
+  std::string key;
+  gnc_fbp_plan *plan = nullptr;
+  float *d_in = nullptr, *d_out = nullptr;
+  unsigned char *h_params = nullptr;  // page-locked parameter block
+  cudaGraphExec_t exec = nullptr;
+  size_t bytes = 0;
+  bool busy = false;
+  bool ready = false;  // created (and its memory held)
+  uint64_t last_use = 0;
+};
+
+struct Request {
+  uint64_t id = 0;
+  gnc_fbp_desc desc{};
+  std::vector<float> angles, centre;
+  std::vector<double> slabs, weights;
+  const float *h_in = nullptr;
+  float *h_out = nullptr;
+  size_t in_bytes = 0, out_bytes = 0, bytes = 0;
+  std::string key;
+  int status = GNC_OK;
+  bool done = false;
+  int graph = 0, device_error = 0;
+  double t_submit = 0, t_start = 0, t_done = 0;
+  std::string error;
+};
+
+struct Slot {
+  cudaStream_t s = nullptr;
+  Request *req = nullptr;
+  Cached *plan = nullptr;
+  int *h_err = nullptr;  // page-locked copy of the plan's device error word
+  bool finished = false;
+  double t_done = 0;
+  gnc_server *srv = nullptr;
+};
+
+}  // namespace
+
+struct gnc_server {
+  int device = 0;
+  size_t budget = 0, used = 0;
+  std::vector<Slot> slots;
+  std::deque<Request *> queue;
+  std::unordered_map<uint64_t, std::unique_ptr<Request>> reqs;
+  std::vector<std::unique_ptr<Cached>> cache;
+  std::mutex mu;
+  std::condition_variable cv_sched, cv_done;
+  std::thread th;
+  bool stop = false, wake = false;
+  uint64_t next_id = 1, tick = 0;
+  int head_skips = 0;
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  cudaStream_t s_cap = nullptr;
+  gnc_server_stats st{};
+
+  double now() const {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+};
+
+namespace {
+
+void CUDART_CB on_done(void *arg) {
+  Slot *sl = static_cast<Slot *>(arg);
+  gnc_server *S = sl->srv;
+  std::lock_guard<std::mutex> lk(S->mu);
+  sl->finished = true;
+  sl->t_done = S->now();
+  S->wake = true;
+  S->cv_sched.notify_one();
+}
+
+void release(Cached *c) {  // CUDA frees: call without the lock
+  if (c->exec) cudaGraphExecDestroy(c->exec);
+  if (c->plan) gnc_fbp_plan_destroy(c->plan);
+  cudaFree(c->d_in);
+  cudaFree(c->d_out);
+  if (c->h_params) cudaFreeHost(c->h_params);
+}
+
+Cached *find_idle(gnc_server *S, const std::string &key) {
+  for (auto &c : S->cache)
+    if (c->ready && !c->busy && c->key == key) return c.get();
+  return nullptr;
+}
+
+size_t idle_bytes(gnc_server *S) {
+  size_t b = 0;
+  for (auto &c : S->cache)
+    if (c->ready && !c->busy) b += c->bytes;
+  return b;
+}
+
+// Under the lock: finish the requests whose slots reported back.
+void reap(gnc_server *S) {
+  for (Slot &sl : S->slots) {
+    if (!sl.req || !sl.finished) continue;
+    Request *r = sl.req;
+    r->t_done = sl.t_done;
+    r->device_error = *sl.h_err != 0;
+    if (r->device_error) {
+      r->status = GNC_ERR_CUDA;
+      r->error = "a bounded wait in a kernel gave up (device error word set)";
+    }
+    r->done = true;
+    sl.plan->busy = false;
+    sl.plan->last_use = ++S->tick;
+    sl.req = nullptr;
+    sl.plan = nullptr;
+    sl.finished = false;
+    S->st.in_flight--;
+    if (r->status == GNC_OK)
+      S->st.completed++;
+    else
+      S->st.failed++;
+  }
+  S->cv_done.notify_all();
+}
+
+void fail(gnc_server *S, Request *r, int status, const std::string &msg) {
+  r->status = status;
+  r->error = msg;
+  r->done = true;
+  r->t_done = S->now();
+  S->st.failed++;
+}
+
+// Without the lock: plan, buffers and parameter block of a new cache entry.
+int create_entry(gnc_server *S, Cached *c, const Request *r) {
+  int st = gnc_fbp_plan_create(&r->desc, &c->plan);
+  if (st != GNC_OK) return st;
+  cudaError_t e = cudaMalloc((void **)&c->d_in, r->in_bytes);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&c->d_out, r->out_bytes);
+  if (e == cudaSuccess)
+    e = cudaHostAlloc((void **)&c->h_params, gnc::plan_param_bytes(c->plan), cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    gnc::set_error(std::string("gnc_server: ") + cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? GNC_ERR_OUT_OF_MEMORY : GNC_ERR_CUDA;
+  }
+  return GNC_OK;
+}
+
+// Without the lock: the launch sequence of c, captured for replay.
+void capture(gnc_server *S, Cached *c) {
+  if (cudaStreamBeginCapture(S->s_cap, cudaStreamCaptureModeRelaxed) != cudaSuccess) return;
+  const int st = gnc_fbp_execute(c->plan, c->d_in, c->d_out, S->s_cap);
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(S->s_cap, &g);
+  if (st == GNC_OK && e == cudaSuccess && g) {
+    cudaGraphExec_t x = nullptr;
+    if (cudaGraphInstantiate(&x, g, 0) == cudaSuccess) c->exec = x;
+  }
+  if (g) cudaGraphDestroy(g);
+  cudaGetLastError();  // a failed capture leaves direct launches in use
+}
+
+// Without the lock: everything one request puts on its slot's stream.
+int enqueue(gnc_server *S, Slot *sl, Request *r, Cached *c, bool *captured_now) {
+  cudaStream_t s = sl->s;
+  int st = gnc::plan_set_request(c->plan, &r->desc, c->h_params, s);
+  if (st != GNC_OK) return st;
+  cudaError_t e = cudaMemcpyAsync(c->d_in, r->h_in, r->in_bytes, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    if (c->exec) {
+      e = cudaGraphLaunch(c->exec, s);
+      r->graph = 1;
+    } else {
+      st = gnc_fbp_execute(c->plan, c->d_in, c->d_out, s);
+      if (st != GNC_OK) return st;
+    }
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(r->h_out, c->d_out, r->out_bytes, cudaMemcpyDeviceToHost, s);
+  int *derr = gnc::plan_error_word(c->plan);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(sl->h_err, derr, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(derr, 0, sizeof(int), s);
+  if (e == cudaSuccess) e = cudaLaunchHostFunc(s, on_done, sl);
+  if (e != cudaSuccess) {
+    gnc::set_error(std::string("gnc_server: ") + cudaGetErrorString(e));
+    return GNC_ERR_CUDA;
+  }
+  if (!c->exec) {
+    capture(S, c);
+    *captured_now = true;
+  }
+  return GNC_OK;
+}
+
+// Under the lock on entry and exit; drops it around the CUDA work.
+void admit(gnc_server *S, std::unique_lock<std::mutex> &lk) {
+  while (!S->stop && !S->queue.empty()) {
+    Slot *sl = nullptr;
+    for (Slot &x : S->slots)
+      if (!x.req) {
+        sl = &x;
+        break;
+      }
+    if (!sl) return;
+    Request *r = nullptr;
+    Cached *c = nullptr;
+    size_t qi = 0;
+    const size_t idle = idle_bytes(S);
+    for (; qi < S->queue.size() && qi < (size_t)kLookAhead; ++qi) {
+      if (qi > 0 && S->head_skips >= kMaxSkips) break;
+      Request *q = S->queue[qi];
+      c = find_idle(S, q->key);
+      if (c || S->used - idle + q->bytes <= S->budget) {
+        r = q;
+        break;
+      }
+    }
+    if (!r) return;
+    S->head_skips = qi == 0 ? 0 : S->head_skips + 1;
+    S->queue.erase(S->queue.begin() + qi);
+    // reserve: an idle plan of the shape, or new memory after releasing idle plans
+    std::vector<std::unique_ptr<Cached>> victims;
+    bool fresh = false;
+    if (!c) {
+      fresh = true;
+      while (S->used + r->bytes > S->budget) {
+        auto lru = S->cache.end();
+        for (auto it = S->cache.begin(); it != S->cache.end(); ++it)
+          if ((*it)->ready && !(*it)->busy &&
+              (lru == S->cache.end() || (*it)->last_use < (*lru)->last_use))
+            lru = it;
+        if (lru == S->cache.end()) break;  // cannot happen: checked above
+        S->used -= (*lru)->bytes;
+        victims.push_back(std::move(*lru));
+        S->cache.erase(lru);
+        S->st.plans_evicted++;
+      }
+      auto nc = std::make_unique<Cached>();
+      nc->key = r->key;
+      nc->bytes = r->bytes;
+      c = nc.get();
+      S->cache.push_back(std::move(nc));
+      S->used += r->bytes;
+    }
+    c->busy = true;
+    sl->req = r;
+    sl->plan = c;
+    sl->finished = false;
+    r->t_start = S->now();
+    S->st.in_flight++;
+    S->st.peak_in_flight = std::max(S->st.peak_in_flight, S->st.in_flight);
+    lk.unlock();
+    for (auto &v : victims) release(v.get());
+    int st = GNC_OK;
+    std::string msg;
+    if (fresh) {
+      st = create_entry(S, c, r);
+      if (st != GNC_OK) msg = gnc::last_error();
+    }
+    bool captured_now = false;
+    const bool replay = c->exec != nullptr;
+    if (st == GNC_OK) {
+      st = enqueue(S, sl, r, c, &captured_now);
+      if (st != GNC_OK) msg = gnc::last_error();
+    }
+    if (st != GNC_OK && fresh) release(c);
+    lk.lock();
+    if (st != GNC_OK) {
+      if (fresh) {
+        S->used -= c->bytes;
+        S->cache.erase(std::find_if(S->cache.begin(), S->cache.end(),
+                                    [c](const std::unique_ptr<Cached> &p) { return p.get() == c; }));
+      } else {
+        c->busy = false;
+      }
+      sl->req = nullptr;
+      sl->plan = nullptr;
+      S->st.in_flight--;
+      fail(S, r, st, msg);
+      S->cv_done.notify_all();
+      continue;
+    }
+    if (fresh) {
+      c->ready = true;
+      S->st.plans_created++;
+    }
+    if (replay)
+      S->st.graph_launches++;
+    else
+      S->st.direct_launches++;
+  }
+}
+
+void run(gnc_server *S) {
+  cudaSetDevice(S->device);
+  std::unique_lock<std::mutex> lk(S->mu);
+  for (;;) {
+    S->cv_sched.wait(lk, [S] { return S->stop || S->wake; });
+    S->wake = false;
+    reap(S);
+    if (S->stop) {
+      bool busy = false;
+      for (Slot &sl : S->slots) busy = busy || sl.req != nullptr;
+      if (!busy) break;
+      continue;
+    }
+    admit(S, lk);
+  }
+}
+
+}  // namespace
+
+using gnc::set_error;
+
+extern "C" {
+
+int gnc_server_create(size_t budget_bytes, int slots, gnc_server **server) {
+  if (!server || slots < 1 || slots > 64 || budget_bytes == 0) {
+    set_error("gnc_server_create: ASSERT (server != nullptr && 1 <= slots <= 64 && budget > 0) failed");
+    return GNC_ERR_INVALID_ARGUMENT;
+  }
+  *server = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    set_error("gnc_server_create: no CUDA device");
+    return GNC_ERR_DEVICE;
+  }
+  auto S = std::make_unique<gnc_server>();
+  cudaGetDevice(&S->device);
+  S->budget = budget_bytes;
+  S->slots.resize(slots);
+  cudaError_t e = cudaStreamCreateWithFlags(&S->s_cap, cudaStreamNonBlocking);
+  for (Slot &sl : S->slots) {
+    sl.srv = S.get();
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sl.s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaHostAlloc((void **)&sl.h_err, sizeof(int), cudaHostAllocDefault);
+  }
+  if (e != cudaSuccess) {
+    set_error(std::string("gnc_server_create: ") + cudaGetErrorString(e));
+    for (Slot &sl : S->slots) {
+      if (sl.s) cudaStreamDestroy(sl.s);
+      if (sl.h_err) cudaFreeHost(sl.h_err);
+    }
+    if (S->s_cap) cudaStreamDestroy(S->s_cap);
+    return GNC_ERR_CUDA;
+  }
+  S->st.budget_bytes = budget_bytes;
+  S->st.slots = slots;
+  gnc_server *raw = S.release();
+  raw->th = std::thread(run, raw);
+  *server = raw;
+  return GNC_OK;
+}
+
+int gnc_server_destroy(gnc_server *S) {
+  if (!S) return GNC_OK;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stop = true;
+    S->wake = true;
+    for (Request *r : S->queue) fail(S, r, GNC_ERR_INVALID_ARGUMENT, "gnc_server: destroyed");
+    S->queue.clear();
+    S->cv_sched.notify_one();
+    S->cv_done.notify_all();
+  }
+  S->th.join();
+  cudaSetDevice(S->device);
+  for (Slot &sl : S->slots) cudaStreamSynchronize(sl.s);
+  for (auto &c : S->cache) release(c.get());
+  for (Slot &sl : S->slots) {
+    cudaStreamDestroy(sl.s);
+    cudaFreeHost(sl.h_err);
+  }
+  cudaStreamDestroy(S->s_cap);
+  delete S;
+  return GNC_OK;
+}
+
+int gnc_server_submit(gnc_server *S, const gnc_fbp_desc *desc, const float *h_input,
+                      float *h_volume, uint64_t *id) {
+  if (!S || !desc || !h_input || !h_volume || !id) {
+    set_error("gnc_server_submit: ASSERT (server && desc && h_input && h_volume && id) failed");
+    return GNC_ERR_INVALID_ARGUMENT;
+  }
+  const int st = gnc::desc_check(desc);
+  if (st != GNC_OK) return st;
+  auto r = std::make_unique<Request>();
+  r->desc = *desc;
+  const size_t T = desc->num_angles, H = desc->height, D = desc->num_defocus;
+  r->angles.assign(desc->angles, desc->angles + T);
+  r->desc.angles = r->angles.data();
+  if (desc->centre) {
+    r->centre.assign(desc->centre, desc->centre + H);
+    r->desc.centre = r->centre.data();
+  }
+  if (desc->slab_defocus) {
+    r->slabs.assign(desc->slab_defocus, desc->slab_defocus + D);
+    r->desc.slab_defocus = r->slabs.data();
+  }
+  if (desc->weights) {
+    r->weights.assign(desc->weights, desc->weights + T);
+    r->desc.weights = r->weights.data();
+  }
+  r->h_in = h_input;
+  r->h_out = h_volume;
+  r->in_bytes = T * (desc->input == GNC_INPUT_CORRECTED ? D : 1) * H * desc->width * sizeof(float);
+  r->out_bytes = H * desc->grid_height * desc->grid_width * sizeof(float);
+  r->bytes = gnc::plan_bytes(desc);
+  r->key = gnc::plan_key(desc);
+  if (r->bytes > S->budget) {
+    set_error("gnc_server_submit: the request needs " + std::to_string(r->bytes) +
+              " device bytes, more than the server's budget of " + std::to_string(S->budget));
+    return GNC_ERR_OUT_OF_MEMORY;
+  }
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (S->stop) {
+    set_error("gnc_server_submit: the server is being destroyed");
+    return GNC_ERR_INVALID_ARGUMENT;
+  }
+  r->id = S->next_id++;
+  r->t_submit = S->now();
+  *id = r->id;
+  S->queue.push_back(r.get());
+  S->reqs.emplace(r->id, std::move(r));
+  S->st.submitted++;
+  S->wake = true;
+  S->cv_sched.notify_one();
+  return GNC_OK;
+}
+
+int gnc_server_wait(gnc_server *S, uint64_t id, double timeout_s, gnc_request_info *info) {
+  if (!S) {
+    set_error("gnc_server_wait: ASSERT (server != nullptr) failed");
+    return GNC_ERR_INVALID_ARGUMENT;
+  }
+  std::unique_lock<std::mutex> lk(S->mu);
+  auto it = S->reqs.find(id);
+  if (it == S->reqs.end()) {
+    set_error("gnc_server_wait: unknown request id " + std::to_string(id));
+    return GNC_ERR_INVALID_ARGUMENT;
+  }
+  Request *r = it->second.get();
+  auto pred = [r] { return r->done; };
+  if (timeout_s < 0)
+    S->cv_done.wait(lk, pred);
+  else
+    S->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), pred);
+  if (!r->done) return GNC_ERR_PENDING;
+  if (info) {
+    info->status = r->status;
+    info->graph = r->graph;
+    info->device_error = r->device_error;
+    info->t_submit = r->t_submit;
+    info->t_start = r->t_start;
+    info->t_done = r->t_done;
+  }
+  const int status = r->status;
+  if (status != GNC_OK) set_error(r->error);
+  S->reqs.erase(it);
+  return status;
+}
+
+double gnc_server_now(const gnc_server *S) { return S ? S->now() : 0.0; }
+
+int gnc_server_get_stats(gnc_server *S, gnc_server_stats *out) {
+  if (!S || !out) {
+    set_error("gnc_server_get_stats: ASSERT (server && stats) failed");
+    return GNC_ERR_INVALID_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> lk(S->mu);
+  *out = S->st;
+  out->bytes_in_use = S->used;
+  out->cached_plans = (int)S->cache.size();
+  out->queued = (int)S->queue.size();
+  return GNC_OK;
+}
+
+}  // extern "C"

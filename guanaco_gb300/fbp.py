@@ -41,9 +41,9 @@ def _stream(stream):
     return stream.cuda_stream
 
 
-class FbpPlan:
-    """3D-CTF FBP of (T, H, W) raw projections or a (T, D, H, W) corrected
-    stack into an (H, Z, X) volume.
+class FbpDesc:
+    """A gnc_fbp_desc (one acquisition geometry and its CTF and volume) with
+    the arrays it points to kept alive.
 
     Parameters mirror the reference's ``correct_projections`` and
     ``reconstruct`` (src/guanaco/detail/correct.py:217-318,
@@ -59,7 +59,6 @@ class FbpPlan:
                  slab_defocus=None, min_defocus=0.0, max_defocus=0.0, energy=300.0,
                  spherical_aberration=0.0, astigmatism=0.0, astigmatism_angle=0.0,
                  phase_shift=0.0, weights=None, minus=False, staging="f32"):
-        self._lib = _lib.load()
         self.T, self.H, self.W = int(num_angles), int(height), int(width)
         self.Z = int(grid_height if grid_height is not None else width)
         self.X = int(grid_width if grid_width is not None else width)
@@ -96,11 +95,8 @@ class FbpPlan:
         d.minus = 1 if minus else 0
         d.staging = _lib.GNC_STAGE_F16 if staging in ("f16", "fp16", "half") else _lib.GNC_STAGE_F32
         self.correcting = bool(d.correct)
-        h = ctypes.c_void_p()
-        _lib.check(self._lib.gnc_fbp_plan_create(ctypes.byref(d), ctypes.byref(h)))
-        self._h = h
+        self.c = d
 
-    # ---------------------------------------------------------------- sizes
     @property
     def input_shape(self):
         if self.input == "raw":
@@ -112,16 +108,30 @@ class FbpPlan:
         return (self.H, self.Z, self.X)
 
     @property
+    def voxel_tilts(self):
+        return self.H * self.Z * self.X * self.T
+
+
+class FbpPlan(FbpDesc):
+    """3D-CTF FBP of (T, H, W) raw projections or a (T, D, H, W) corrected
+    stack into an (H, Z, X) volume, with the device workspace of one
+    geometry (parameters as FbpDesc)."""
+
+    def __init__(self, num_angles, height, width, angles, **kw):
+        super().__init__(num_angles, height, width, angles, **kw)
+        self._lib = _lib.load()
+        h = ctypes.c_void_p()
+        _lib.check(self._lib.gnc_fbp_plan_create(ctypes.byref(self.c), ctypes.byref(h)))
+        self._h = h
+
+    # ---------------------------------------------------------------- sizes
+    @property
     def workspace_bytes(self):
         return self._lib.gnc_fbp_workspace_bytes(self._h)
 
     @property
     def launches_per_execute(self):
         return self._lib.gnc_fbp_launches(self._h)
-
-    @property
-    def voxel_tilts(self):
-        return self.H * self.Z * self.X * self.T
 
     # ------------------------------------------------------------- running
     def execute(self, inp, vol, stream=None):

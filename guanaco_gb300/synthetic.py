@@ -94,3 +94,31 @@ def _wavelength(V):
     c, e, m_e, h = 2.99792458e8, 1.602176634e-19, 9.1093837015e-31, 6.62607004e-34
     eV = e * V
     return h * c / math.sqrt(eV * eV + 2 * m_e * eV * c * c) * 1e10
+
+
+def request_stream(num_requests, rate_hz, seed, sizes=(128, 256, 384, 512), tilts=(31, 41, 61),
+                   defocus=(10000.0, 50000.0), max_ndf=10, f16_fraction=0.5):
+    """A seeded stream of serving requests: Poisson arrivals at ``rate_hz``;
+    per request a square projection size from ``sizes``, a tilt count from
+    ``tilts`` (over +-60 deg), a defocus uniform in ``defocus`` (A), a slab
+    count uniform in 1..max_ndf, FP16 staging with probability
+    ``f16_fraction``, volume thickness size / 2, and a phantom seed.  Returns a
+    list of dicts sorted by arrival time (s, from 0)."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate_hz, num_requests)
+    arrival = np.cumsum(gaps) - gaps[0]
+    out = []
+    for i in range(num_requests):
+        n = int(rng.choice(sizes))
+        out.append({
+            "id": i,
+            "arrival": float(arrival[i]),
+            "size": n,
+            "tilts": int(rng.choice(tilts)),
+            "defocus": float(rng.uniform(defocus[0], defocus[1])),
+            "ndf": int(rng.integers(1, max_ndf + 1)),
+            "staging": "f16" if rng.random() < f16_fraction else "f32",
+            "thickness": n // 2,
+            "seed": int(seed * 1000003 + i),
+        })
+    return out

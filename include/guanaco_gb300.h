@@ -37,7 +37,8 @@ typedef enum {
   GNC_ERR_UNSUPPORTED = 2,      /* valid for the reference, not built here (message says why) */
   GNC_ERR_CUDA = 3,             /* CUDA runtime error (message has cudaGetErrorString) */
   GNC_ERR_OUT_OF_MEMORY = 4,
-  GNC_ERR_DEVICE = 5            /* device path requested on a machine without a usable GPU */
+  GNC_ERR_DEVICE = 5,           /* device path requested on a machine without a usable GPU */
+  GNC_ERR_PENDING = 6           /* gnc_server_wait: the request has not finished yet */
 } gnc_status;
 
 /* Message of the last failed call on this thread ("" if none). */
@@ -229,6 +230,63 @@ GNC_API int gnc_fbp_check(gnc_fbp_plan *plan, void *stream);
 /* Staged filtered rows: (ceil(H/2), D, T, W) pairs of float (F32) or half (F16),
  * and for F16 the (ceil(H/2), D, T, 2) int8 row exponents (value = half * 2^-e). */
 GNC_API int gnc_fbp_staged(gnc_fbp_plan *plan, const void **d_staged, const int8_t **d_row_exp);
+
+/* ------------------------------------------------------------------------
+ * Request server: continuous batching of whole-series FBP requests on one GPU.
+ * No counterpart in the reference, which runs one synchronous call at a time
+ * (src/guanaco/detail/mp.py:38-153 loops over rows inside one request).
+ *
+ * Requests (a gnc_fbp_desc plus host input and output buffers) are queued by
+ * gnc_server_submit and admitted by a scheduler thread whenever one of the
+ * server's slots (CUDA streams) is free and the request's plan fits in the
+ * device-memory budget; requests of different sizes and parameters run
+ * concurrently on the slots.  Plans are cached by shape (gnc_fbp_desc minus
+ * the per-request values: angles, centres, defocus, CTF constants, weights)
+ * and the device work of a cached plan is captured once as a CUDA graph; a
+ * later request of that shape uploads its parameters and replays the graph.
+ * Idle cached plans are released (least recently used first) when a new shape
+ * needs the memory.  Page-locked host buffers let the copies run
+ * asynchronously; the buffers must stay valid until gnc_server_wait reports
+ * the request finished.
+ * ---------------------------------------------------------------------- */
+typedef struct gnc_server gnc_server;
+
+typedef struct {
+  int status;          /* GNC_OK, or the request's error (gnc_server_wait returns it too) */
+  int graph;           /* 1: ran as a replay of a captured graph, 0: direct launches */
+  int device_error;    /* a bounded wait in a kernel gave up (status GNC_ERR_CUDA) */
+  double t_submit;     /* seconds on the server clock (gnc_server_now) */
+  double t_start;      /* admitted: parameters, input copy and kernels enqueued */
+  double t_done;       /* volume back in the host buffer */
+} gnc_request_info;
+
+typedef struct {
+  uint64_t submitted, completed, failed;
+  uint64_t graph_launches, direct_launches, plans_created, plans_evicted;
+  size_t budget_bytes, bytes_in_use;
+  int slots, cached_plans, in_flight, peak_in_flight, queued;
+} gnc_server_stats;
+
+/* Creates a server on the current device with `slots` concurrent requests
+ * (1..64) and a device-memory budget for its plans and request buffers. */
+GNC_API int gnc_server_create(size_t budget_bytes, int slots, gnc_server **server);
+/* Waits for every admitted request, then frees everything; queued requests
+ * that were never admitted finish with GNC_ERR_INVALID_ARGUMENT. */
+GNC_API int gnc_server_destroy(gnc_server *server);
+/* Queues one request: desc as for gnc_fbp_plan_create (its arrays are copied),
+ * h_input (T, H, W) raw or (T, D, H, W) corrected float32, h_volume (H, Z, X)
+ * float32 written when the request finishes.  Invalid or unsupported
+ * descriptors, and requests larger than the whole budget, fail here. */
+GNC_API int gnc_server_submit(gnc_server *server, const gnc_fbp_desc *desc, const float *h_input,
+                              float *h_volume, uint64_t *id);
+/* Waits up to timeout_s seconds (< 0: forever) for request id.  Returns
+ * GNC_ERR_PENDING if it has not finished, else its status, and fills info
+ * (may be NULL); a finished request is forgotten after this call. */
+GNC_API int gnc_server_wait(gnc_server *server, uint64_t id, double timeout_s,
+                            gnc_request_info *info);
+/* Seconds since the server was created (the clock of gnc_request_info). */
+GNC_API double gnc_server_now(const gnc_server *server);
+GNC_API int gnc_server_get_stats(gnc_server *server, gnc_server_stats *stats);
 
 #ifdef __cplusplus
 }
