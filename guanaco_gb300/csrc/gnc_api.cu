@@ -330,8 +330,7 @@ size_t plan_bytes(const gnc_fbp_desc *d) {
     const size_t chunk = std::max<size_t>(1, std::min<size_t>(T, (48ull << 20) / per_tilt));
     b += T * H * half * sizeof(float2) + chunk * D * H * half * sizeof(float2) + D * H * (half + 1);
   }
-  const size_t pb = d->staging == GNC_STAGE_F16 ? sizeof(__half2) : sizeof(float2);
-  b += (Y2 * D * T * W + 8) * pb;
+  b += (Y2 * D * T * W + 8) * kStagedPixelBytes;
   if (d->staging == GNC_STAGE_F16) b += Y2 * D * T * 2;
   const size_t in_elems = T * (d->input == GNC_INPUT_CORRECTED ? D : 1) * H * W;
   b += (in_elems + H * d->grid_height * d->grid_width) * sizeof(float);
@@ -434,7 +433,7 @@ int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
   // +8 pixels: a 16-byte aligned bulk copy of the last row may run past its end
   const size_t elems = (size_t)p->Y2 * p->D * p->T * p->W + 8;
   if (e == cudaSuccess)
-    e = p->staging == GNC_STAGE_F16 ? dalloc(p, (__half2 **)&p->staged, elems)
+    e = p->staging == GNC_STAGE_F16 ? dalloc(p, (uint2 **)&p->staged, elems)
                                     : dalloc(p, (float2 **)&p->staged, elems);
   if (e == cudaSuccess && p->staging == GNC_STAGE_F16)
     e = dalloc(p, &p->row_exp, (size_t)p->Y2 * p->D * p->T * 2);
@@ -615,7 +614,7 @@ static int execute_host_pipelined(gnc_fbp_plan *p, const float *h_input, float *
   }
   // backprojection in slabs of whole row pairs, each copied out when done
   const int rows = ((p->H + 7) / 8 + 7) / 8 * 8;  // at most 8 slabs of whole block rows
-  const size_t pb = p->staging == GNC_STAGE_F16 ? sizeof(__half2) : sizeof(float2);
+  const size_t pb = kStagedPixelBytes;
   for (int j = 0, y0 = 0; y0 < p->H; ++j, y0 += rows) {
     const int ny = std::min(rows, p->H - y0);
     BpArgs a = bp_args(p, p->io_out + (size_t)y0 * plane);

@@ -53,9 +53,11 @@ __global__ void k_bp_exact(BpArgs a) {
       const float tt = __fsub_rn(pixel, (float)ind);
       if (ind >= 0 && ind < a.N - 1) {
         float v0, v1;
-        if (F16) {
-          const __half2 *row = (const __half2 *)a.staged + rowi * a.N;
-          float2 p0 = __half22float2(row[ind]), p1 = __half22float2(row[ind + 1]);
+        if (F16) {  // the values of records ind and ind + 1
+          const uint2 *row = (const uint2 *)a.staged + rowi * a.N;
+          const unsigned u0 = row[ind].x, u1 = row[ind + 1].x;
+          float2 p0 = __half22float2(*(const __half2 *)&u0);
+          float2 p1 = __half22float2(*(const __half2 *)&u1);
           v0 = (r == 0 ? p0.x : p0.y) * (r == 0 ? sa : sb);
           v1 = (r == 0 ? p1.x : p1.y) * (r == 0 ? sa : sb);
         } else {

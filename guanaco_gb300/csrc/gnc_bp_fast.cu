@@ -23,9 +23,13 @@
 // shared-memory buffer, tracked by an mbarrier.  Two buffers alternate, so
 // group g+1 is in flight while group g is accumulated.
 //
-// FP32 staging: v0, v1 are two 8-byte loads; FP16 staging: two 4-byte loads,
-// the interpolation is one half2 FMA and the sum one f32x2 FMA with
-// (scale 2^-e_a, scale 2^-e_b) for that row pair and slab.
+// FP32 staging: v0, v1 are two 8-byte loads, the interpolation and the sum
+// f32x2 operations.  FP16 staging: one 8-byte load of the pixel's record
+// (both rows' values and differences to the next pixel), the interpolation
+// one half2 FMA and the sum one f32x2 FMA with (scale 2^-e_a, scale 2^-e_b)
+// for that row pair and slab.  The FP16 form reads half the shared-memory
+// bytes per voxel-tilt; it holds 4 voxels x 16 rows per thread (FP32: 8 x 8)
+// so that the per-voxel work is shared by more rows.
 #include <cmath>
 
 #include "gnc_common.cuh"
@@ -131,12 +135,13 @@ struct TiltParams {
 
 template <int RP, int KMAX, int G, bool F16>
 struct FastBp {
-  static constexpr int A = 2, B = 4;              // voxels per thread in x and z
+  static constexpr int A = 2, B = F16 ? 2 : 4;    // voxels per thread in x and z
+  static constexpr int TCH = RP * KMAX > 16 ? 64 : 128;  // tilts whose parameters are held
   static constexpr int WX = 4, WZ = 2;            // warps per block in x and z
   static constexpr int TX = 4 * A * WX;           // tile width (x)
   static constexpr int TZ = 8 * B * WZ;           // tile height (z)
   static constexpr int NT = 32 * WX * WZ;         // threads
-  static constexpr int PB = F16 ? 4 : 8;          // bytes per staged pixel (both rows)
+  static constexpr int PB = kStagedPixelBytes;    // bytes per staged pixel (both rows)
   static constexpr int ALIGN = 16 / PB;           // pixels per 16 bytes
   // widest detector window of a TX x TZ tile: (TX-1)|c| + (TZ-1)|s| <=
   // sqrt(TX^2 + TZ^2); plus the right neighbour and slack
@@ -161,7 +166,7 @@ k_bp_fast(BpArgs a) {
     a.doffset = a.dyn[1];
   }
   constexpr int A = P::A, B = P::B;
-  constexpr int TCH = 128;  // tilts whose parameters are held at once
+  constexpr int TCH = P::TCH;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ TiltParams s_tp[TCH];
   __shared__ float2 s_rs[TCH * RP * KMAX];  // per (tilt, row pair, slab) scale
@@ -389,8 +394,9 @@ k_bp_fast(BpArgs a) {
 #pragma unroll
               for (int rr = 0; rr < RP; ++rr) {
                 const unsigned char *p = p0 + rr * KMAX * P::SLOT_BYTES;
-                const __half2 v0 = *(const __half2 *)p, v1 = *(const __half2 *)(p + 4);
-                const float2 val = __half22float2(__hfma2(t2, __hsub2(v1, v0), v0));
+                const uint2 rec = *(const uint2 *)p;  // (v_a, v_b), (dv_a, dv_b)
+                const __half2 v0 = *(const __half2 *)&rec.x, dv = *(const __half2 *)&rec.y;
+                const float2 val = __half22float2(__hfma2(t2, dv, v0));
                 u64 sc = rs[rr];
                 if (!uniform) {
                   const float2 f = trs[rr * KMAX + c];
@@ -460,7 +466,7 @@ bool backproject_fast_supported(const BpArgs &a) {
   using P = FastBp<4, 2, 8, false>;
   // 16-byte aligned staged rows for the bulk copies; the fast path covers up to
   // four slabs per tile and a shared centre
-  const int align_px = a.staging == kStageF16 ? 4 : 2;
+  const int align_px = 16 / kStagedPixelBytes;
   return a.uniform_centre && a.N % align_px == 0 && max_slabs_per_tile(a, P::TX, P::TZ) <= 4 &&
          a.N >= 2;
 }
@@ -476,9 +482,11 @@ cudaError_t launch_backproject_fast(const BpArgs &a, cudaStream_t s) {
   if (!backproject_fast_supported(a)) return launch_backproject_exact(a, s);
   const int need = max_slabs_per_tile(a, P::TX, P::TZ);
   const bool f16 = a.staging == kStageF16;
+  // <row pairs per thread, slabs per tile, tilts per group>: two buffers of
+  // G * RP * KMAX slots within two blocks per SM
   if (need <= 2)
-    return f16 ? launch_fast<4, 2, 8, true>(a, s) : launch_fast<4, 2, 8, false>(a, s);
-  return f16 ? launch_fast<4, 4, 4, true>(a, s) : launch_fast<4, 4, 4, false>(a, s);
+    return f16 ? launch_fast<8, 2, 6, true>(a, s) : launch_fast<4, 2, 8, false>(a, s);
+  return f16 ? launch_fast<8, 4, 3, true>(a, s) : launch_fast<4, 4, 4, false>(a, s);
 }
 
 }  // namespace gnc

@@ -23,6 +23,24 @@ bool fft_length_supported(long n);
 // ---- staging element types ------------------------------------------------
 enum Staging : int { kStageF32 = 0, kStageF16 = 1 };
 
+// One staged detector pixel n of a row pair (rows a = 2 y2, b = 2 y2 + 1):
+//   F32: float2 (v_a, v_b)                                              8 bytes
+//   F16: half2 (v_a, v_b) and half2 (v_a[n+1] - v_a[n], v_b[n+1] - v_b[n]),
+//        each row scaled by its 2^e, the difference taken between the two
+//        rounded FP16 values (0 for the last pixel), so the backprojector's
+//        interpolation is one load and one half2 FMA                    8 bytes
+constexpr int kStagedPixelBytes = 8;
+// v0, v1: pixels n and n + 1 already multiplied by the rows' 2^e
+__device__ __forceinline__ uint2 staged_record_f16(float2 v0, float2 v1) {
+  const __half2 h0 = __floats2half2_rn(v0.x, v0.y), h1 = __floats2half2_rn(v1.x, v1.y);
+  const float2 f0 = __half22float2(h0), f1 = __half22float2(h1);
+  const __half2 dv = __floats2half2_rn(f1.x - f0.x, f1.y - f0.y);
+  uint2 r;
+  r.x = *(const unsigned *)&h0;
+  r.y = *(const unsigned *)&dv;
+  return r;
+}
+
 // Per-tilt backprojection geometry, computed on the host with the reference's
 // float arithmetic (src/libguanaco/reconstructor.cpp:35-47).
 struct TiltGeom {
@@ -91,7 +109,7 @@ struct RowStageArgs {
   // output
   int out_staged;        // 1: staged pairs (Y2, D, T, N), 0: plain rows
   int staging;           // kStageF32 / kStageF16 when out_staged
-  void *staged;          // float2 or __half2
+  void *staged;          // float2 pairs or FP16 records
   int8_t *row_exp;       // (Y2, D, T, 2) FP16 exponents when staging == F16
   float *out_rows;       // plain rows: (nt, D, H, N) at [t][d][y][n]
 };
@@ -99,7 +117,7 @@ cudaError_t launch_row_stage(const RowStageArgs &a, cudaStream_t s);
 
 // Backprojection of the staged pairs into the volume (Y, Z, X).
 struct BpArgs {
-  const void *staged;     // (Y2, D, T, N) float2 / __half2
+  const void *staged;     // (Y2, D, T, N) float2 pairs / FP16 records
   const int8_t *row_exp;  // F16 exponents or null
   int staging;
   int Y, D, T, N, Z, X;

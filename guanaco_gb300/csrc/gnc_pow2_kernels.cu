@@ -272,6 +272,12 @@ __global__ void __launch_bounds__(256) k_row_p2(RowStageArgs a, const float2 *__
       for (int m = 0; m < 16; ++m) dst[j + m * P::NT] = yv[m];
     }
   } else if (STAGED && F16) {
+    // the records need pixel n + 1, held by another thread: exchange the
+    // group's row pair through its (no longer needed) transform buffer
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < 16; ++m) zb[fpad(j + m * P::NT)] = yv[m];
+    __syncthreads();
     float ma = 0.f, mb = 0.f;
 #pragma unroll
     for (int m = 0; m < 16; ++m) {
@@ -303,9 +309,14 @@ __global__ void __launch_bounds__(256) k_row_p2(RowStageArgs a, const float2 *__
     const float sa = __int_as_float((127 + e_a) << 23), sb = __int_as_float((127 + e_b) << 23);
     if (active) {
       const size_t rowi = ((size_t)y2 * a.D + d) * a.T + t;
-      __half2 *dst = (__half2 *)a.staged + rowi * N;
+      uint2 *dst = (uint2 *)a.staged + rowi * N;
 #pragma unroll
-      for (int m = 0; m < 16; ++m) dst[j + m * P::NT] = __floats2half2_rn(yv[m].x * sa, yv[m].y * sb);
+      for (int m = 0; m < 16; ++m) {
+        const int n = j + m * P::NT;
+        const float2 v1 = n + 1 < N ? zb[fpad(n + 1)] : yv[m];
+        dst[n] = staged_record_f16(make_float2(yv[m].x * sa, yv[m].y * sb),
+                                   make_float2(v1.x * sa, v1.y * sb));
+      }
       if (j == 0) {
         a.row_exp[2 * rowi] = (int8_t)e_a;
         a.row_exp[2 * rowi + 1] = (int8_t)e_b;

@@ -138,12 +138,15 @@ __global__ void k_row_stage(RowStageArgs a, FftPlan planN, FftPlan plan2N, int r
       eb = max(-120, min(120, eb));
       float sa = __int_as_float((127 + ea) << 23), sb = __int_as_float((127 + eb) << 23);
       size_t rowi = ((size_t)y2 * a.D + d) * a.T + t;
-      __half2 *dst = (__half2 *)a.staged + rowi * N;
-      for (int n = threadIdx.x; n < N; n += blockDim.x) {
-        float2 v = row[n];
+      uint2 *dst = (uint2 *)a.staged + rowi * N;
+      // the output value of pixel n (n + 1 past the end: the last pixel itself)
+      auto value = [&](int n) {
+        float2 v = row[n < N ? n : N - 1];
         if (RAMP) v = make_float2(v.x / out_scale, v.y / out_scale);
-        dst[n] = __floats2half2_rn(v.x * f * sa, v.y * f * sb);
-      }
+        return make_float2(v.x * f * sa, v.y * f * sb);
+      };
+      for (int n = threadIdx.x; n < N; n += blockDim.x)
+        dst[n] = staged_record_f16(value(n), value(n + 1));
       if (threadIdx.x == 0) {
         a.row_exp[2 * rowi] = (int8_t)ea;
         a.row_exp[2 * rowi + 1] = (int8_t)eb;

@@ -149,7 +149,8 @@ __global__ void __launch_bounds__(256, 2) k_column_w1024(const float2 *__restric
 // Row stage for 1024-pixel rows: one warp per row pair.
 // The input is parked in shared memory; the odd path (c, twist, FFT, w_odd,
 // IFFT, untwist / 2N) runs in registers and trades places with it; then the
-// even path runs on the parked input and adds the odd result.
+// even path runs on the parked input and adds the odd result.  The ramp's
+// four transforms are one forward transform run in a loop.
 // ---------------------------------------------------------------------------
 template <bool SPECTRA, bool RAMP, bool STAGED, bool F16>
 __global__ void __launch_bounds__(128, 3) k_row_w1024(RowStageArgs a,
@@ -209,45 +210,85 @@ __global__ void __launch_bounds__(128, 3) k_row_w1024(RowStageArgs a,
 #pragma unroll
     for (int m = 0; m < 32; ++m) vb[32 * m + lane] = v[m];
   }
-  if (SPECTRA) warp_fft1024<true>(v, tb, tw, lane);  // c = IFFT(Z)
-  if (RAMP) {
-    // odd bins: FFT(c exp(-i pi n / N)) * w_odd, inverse, times exp(+i pi n / N) / 2N
+  if (!RAMP) {
+    if (SPECTRA) warp_fft1024<true>(v, tb, tw, lane);  // the corrected rows: IFFT(Z)
+  } else {
+    // Four transforms, all run as one forward transform in a loop (one copy of
+    // its code): IFFT(x) = conj(FFT(conj(x))), the conjugations folded into
+    // the pointwise steps between the passes.
+    //   spectra in: IFFT(Z) -> c; FFT(c e^{-i pi n/N}) * w_odd; IFFT -> odd term;
+    //               IFFT(w_even Z) -> even term
+    //   rows in:    FFT(c e^{-i pi n/N}) * w_odd; IFFT -> odd term; FFT(c) * w_even;
+    //               IFFT -> even term
+    if (SPECTRA) {
 #pragma unroll
-    for (int m = 0; m < 32; ++m) v[m] = cmul(v[m], __ldg(roots2N + 32 * m + lane));
-    warp_fft1024<false>(v, tb, tw, lane);
+      for (int m = 0; m < 32; ++m) v[m].y = -v[m].y;
+    } else {
 #pragma unroll
-    for (int m = 0; m < 32; ++m) {
-      const float wo = ramp_w1024(2 * (32 * m + lane) + 1);
-      v[m] = make_float2(wo * v[m].x, wo * v[m].y);
+      for (int m = 0; m < 32; ++m) v[m] = cmul(v[m], __ldg(roots2N + 32 * m + lane));
     }
-    warp_fft1024<true>(v, tb, tw, lane);
-    // swap: the odd-path result goes to the parking slots, the input comes back
+    const int first_odd = SPECTRA ? 1 : 0;  // pass whose output is FFT(c twist)
+#pragma unroll 1
+    for (int ps = 0; ps < 4; ++ps) {
+      warp_fft1024<false>(v, tb, tw, lane);
+      __syncwarp();
+      if (ps == 3) {
+        // even term: IFFT = conj of this pass; y = ea * even + odd
+        const float ea = SPECTRA ? 0.5f : 0.5f * kInvN;
 #pragma unroll
-    for (int m = 0; m < 32; ++m) {
-      const float2 r2 = __ldg(roots2N + 32 * m + lane);
-      const float2 o = cmul(make_float2(r2.x, -r2.y), v[m]);
-      v[m] = vb[32 * m + lane];
-      vb[32 * m + lane] = make_float2(o.x * (0.5f * kInvN), o.y * (0.5f * kInvN));
-    }
-    // even bins: w_even FFT_N(c) = N w_even Z
-    if (!SPECTRA) warp_fft1024<false>(v, tb, tw, lane);
+        for (int m = 0; m < 32; ++m) {
+          const float2 o = vb[32 * m + lane];
+          v[m] = make_float2(ea * v[m].x + o.x, o.y - ea * v[m].y);
+        }
+      } else if (SPECTRA && ps == 0) {
+        // c = conj(v); twist: c e^{-i pi n / N}
 #pragma unroll
-    for (int m = 0; m < 32; ++m) {
-      const float we = ramp_w1024(2 * (32 * m + lane));
-      v[m] = make_float2(we * v[m].x, we * v[m].y);
-    }
-    warp_fft1024<true>(v, tb, tw, lane);
-    const float ea = SPECTRA ? 0.5f : 0.5f * kInvN;
+        for (int m = 0; m < 32; ++m)
+          v[m] = cmul(make_float2(v[m].x, -v[m].y), __ldg(roots2N + 32 * m + lane));
+      } else if (ps == first_odd) {
+        // odd bins times w_odd, conjugated for the inverse
 #pragma unroll
-    for (int m = 0; m < 32; ++m) {
-      const float2 o = vb[32 * m + lane];
-      v[m] = make_float2(ea * v[m].x + o.x, ea * v[m].y + o.y);
+        for (int m = 0; m < 32; ++m) {
+          const float wo = ramp_w1024(2 * (32 * m + lane) + 1);
+          v[m] = make_float2(wo * v[m].x, -wo * v[m].y);
+        }
+      } else if (ps == first_odd + 1) {
+        // odd term conj(v) e^{+i pi n / N} / 2N to the parking slots; the input
+        // comes back (spectra: Z, then w_even Z conjugated for the inverse)
+#pragma unroll
+        for (int m = 0; m < 32; ++m) {
+          const float2 r2 = __ldg(roots2N + 32 * m + lane);
+          const float2 o = cmul(make_float2(r2.x, -r2.y), make_float2(v[m].x, -v[m].y));
+          v[m] = vb[32 * m + lane];
+          vb[32 * m + lane] = make_float2(o.x * (0.5f * kInvN), o.y * (0.5f * kInvN));
+          if (SPECTRA) {
+            const float we = ramp_w1024(2 * (32 * m + lane));
+            v[m] = make_float2(we * v[m].x, -we * v[m].y);
+          }
+        }
+      } else {
+        // rows in, after FFT(c): w_even, conjugated for the inverse
+#pragma unroll
+        for (int m = 0; m < 32; ++m) {
+          const float we = ramp_w1024(2 * (32 * m + lane));
+          v[m] = make_float2(we * v[m].x, -we * v[m].y);
+        }
+      }
     }
   }
   float2 *y = v;
   const float f = a.tilt_factor ? a.tilt_factor[t] : 1.0f;
 #pragma unroll
   for (int m = 0; m < 32; ++m) y[m] = make_float2(y[m].x * f, y[m].y * f);
+  // pixel 32 m + lane + 1 of the row pair: the next lane's element m, or lane
+  // 0's element m + 1 for lane 31 (the last pixel is its own neighbour)
+  auto next_px = [&](const float2 *w, int m) {
+    const float2 src = (lane == 0 && m < 31) ? w[m < 31 ? m + 1 : m] : w[m];
+    float2 nb;
+    nb.x = __shfl_sync(0xffffffffu, src.x, (lane + 1) & 31);
+    nb.y = __shfl_sync(0xffffffffu, src.y, (lane + 1) & 31);
+    return (m == 31 && lane == 31) ? w[m] : nb;
+  };
   if (STAGED && !F16) {
     float2 *dst = (float2 *)a.staged + (((size_t)y2 * a.D + d) * a.T + t) * kN;
 #pragma unroll
@@ -272,9 +313,11 @@ __global__ void __launch_bounds__(128, 3) k_row_w1024(RowStageArgs a,
     e_b = max(-120, min(120, e_b));
     const float sa = __int_as_float((127 + e_a) << 23), sb = __int_as_float((127 + e_b) << 23);
     const size_t rowi = ((size_t)y2 * a.D + d) * a.T + t;
-    __half2 *dst = (__half2 *)a.staged + rowi * kN;
+    uint2 *dst = (uint2 *)a.staged + rowi * kN;
 #pragma unroll
-    for (int m = 0; m < 32; ++m) dst[32 * m + lane] = __floats2half2_rn(y[m].x * sa, y[m].y * sb);
+    for (int m = 0; m < 32; ++m) y[m] = make_float2(y[m].x * sa, y[m].y * sb);
+#pragma unroll
+    for (int m = 0; m < 32; ++m) dst[32 * m + lane] = staged_record_f16(y[m], next_px(y, m));
     if (lane == 0) {
       a.row_exp[2 * rowi] = (int8_t)e_a;
       a.row_exp[2 * rowi + 1] = (int8_t)e_b;
