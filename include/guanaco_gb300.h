@@ -227,8 +227,12 @@ GNC_API int gnc_fbp_launches(const gnc_fbp_plan *plan);
  * plan's kernels: every wait in them is bounded and records a timeout here
  * instead of hanging. */
 GNC_API int gnc_fbp_check(gnc_fbp_plan *plan, void *stream);
-/* Staged filtered rows: (ceil(H/2), D, T, W) pairs of float (F32) or half (F16),
- * and for F16 the (ceil(H/2), D, T, 2) int8 row exponents (value = half * 2^-e). */
+/* Staged filtered rows, (ceil(H/2), D, T, W) pixels of row pairs (rows 2 y2 and
+ * 2 y2 + 1), 8 bytes each:
+ *   F32: float (v_a, v_b)
+ *   F16: half (v_a, v_b, dv_a, dv_b), dv the difference of the next pixel's FP16
+ *        value and this one (0 for the last pixel), value = half * 2^-e;
+ *        with the (ceil(H/2), D, T, 2) int8 row exponents e. */
 GNC_API int gnc_fbp_staged(gnc_fbp_plan *plan, const void **d_staged, const int8_t **d_row_exp);
 
 /* ------------------------------------------------------------------------
