@@ -203,6 +203,51 @@ def test_exact_backprojector_bit_exact(torch, oracle):
         np.testing.assert_array_equal(got[y], ref)
 
 
+def _f16_records(filt, H, exps):
+    """FP16 staged records (H2, D, T, W, 4) = (v_a, v_b, dv_a, dv_b) of rows scaled
+    by 2^exps[y, d, t], and the int8 exponents (H2, D, T, 2)."""
+    _, D, T, W = filt.shape
+    H2 = (H + 1) // 2
+    rec = np.zeros((H2, D, T, W, 4), np.float16)
+    rexp = np.zeros((H2, D, T, 2), np.int8)
+    for y in range(H):
+        e = exps[y]
+        v = (filt[y] * np.exp2(e).astype(np.float32)[..., None]).astype(np.float16)
+        dv = np.zeros_like(v)
+        dv[..., :-1] = (v[..., 1:].astype(np.float32) - v[..., :-1].astype(np.float32)).astype(
+            np.float16)
+        rec[y // 2, ..., y % 2] = v
+        rec[y // 2, ..., 2 + y % 2] = dv
+        rexp[y // 2, ..., y % 2] = e
+    return rec, rexp
+
+
+# The FP16 backprojector brings every slab of a row pair to one reference
+# exponent in shared memory (exact powers of two): the same values staged with
+# other per-slab exponents must give the same volume bit for bit, and the
+# result must match the exact backprojector on the same FP16 values.
+def test_fp16_slab_exponents_are_exact(torch, oracle):
+    T, H, W, Z, D = 13, 10, 64, 48, 6
+    plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=T, H=H, W=W, Z=Z, D=D, seed=5,
+                                                 staging="f16")
+    rng = np.random.default_rng(11)
+    filt = (rng.uniform(0.5, 1.0, (H, D, T, W)) * rng.choice([-1.0, 1.0], (H, D, T, W)))
+    filt = (filt * np.exp2(3.0 * np.arange(D))[None, :, None, None]).astype(np.float32)
+    natural = 13 - np.floor(np.log2(np.abs(filt).max(axis=-1))).astype(np.int64)
+    shifted = natural - 2 * np.arange(D)[None, :, None]  # slab-dependent, still normal FP16
+    vols = []
+    for exps in (natural, shifted):
+        rec, rexp = _f16_records(filt, H, exps)
+        vol = torch.empty((H, Z, W), dtype=torch.float32, device="cuda")
+        plan.backproject_staged(dev(torch, rec), dev(torch, rexp), vol, exact=False)
+        vols.append(vol.cpu().numpy())
+    np.testing.assert_array_equal(vols[1], vols[0])
+    rec, rexp = _f16_records(filt, H, natural)
+    exact = torch.empty((H, Z, W), dtype=torch.float32, device="cuda")
+    plan.backproject_staged(dev(torch, rec), dev(torch, rexp), exact, exact=True)
+    assert rel_l2(vols[0], exact.cpu().numpy()) < 5e-4
+
+
 # ---------------------------------------------------------- whole pipeline
 def _oracle_volume(oracle, proj, ang, c, ctf, mn, mx, Z, precision, weights=None, minus=False):
     return oracle.fbp_ctf(proj, ang, c, 1.0, ctf, mn, mx, weights, minus, Z=Z,
