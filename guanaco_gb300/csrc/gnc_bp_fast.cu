@@ -31,6 +31,7 @@
 // bytes per voxel-tilt; it holds 4 voxels x 16 rows per thread (FP32: 8 x 8)
 // so that the per-voxel work is shared by more rows.
 #include <cmath>
+#include <type_traits>
 
 #include "gnc_common.cuh"
 
@@ -123,6 +124,12 @@ constexpr int isqrt_ceil(int v) {
   return r;
 }
 
+constexpr unsigned kHalf2One = 0x3C003C00u;  // half2 (1, 1)
+// FP16 bits of 2^-k for k >= 0 (subnormal from k = 15, 0 beyond k = 24)
+__device__ __forceinline__ unsigned half_pow2_neg(int k) {
+  return k <= 14 ? (unsigned)(15 - k) << 10 : (k <= 24 ? 1u << (24 - k) : 0u);
+}
+
 struct TiltParams {
   float cos_a, sin_a, off, scale;
   int p_s;      // first staged pixel (aligned down for the bulk copy)
@@ -169,7 +176,12 @@ k_bp_fast(BpArgs a) {
   constexpr int TCH = P::TCH;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ TiltParams s_tp[TCH];
-  __shared__ float2 s_rs[TCH * RP * KMAX];  // per (tilt, row pair, slab) scale
+  // FP16: per (tilt, row pair) the BP scale times 2^-e of the row pair's
+  // reference exponent (the smallest over the tile's slabs), and per (tilt,
+  // row pair, slab) the half2 power of two 2^(e_ref - e) that brings that
+  // slab's staged values to the reference (1 for most slots)
+  __shared__ float2 s_rs[F16 ? TCH * RP : 1];
+  __shared__ unsigned s_fac[F16 ? TCH * RP * KMAX : 1];
   __shared__ __align__(8) u64 s_bar[2];
 
   const int tid = threadIdx.x;
@@ -279,23 +291,33 @@ k_bp_fast(BpArgs a) {
       tp.pad = min(p_hi + 1, a.N - 1);
       s_tp[tl] = tp;
     }
-    // scale per (tilt, row pair, slab): the BP scale, times 2^-e of each row (F16)
-    for (int e = tid; e < nch * RP * KMAX; e += P::NT) {
-      const float sc = a.geom[tbase + e / (RP * KMAX)].scale;
-      s_rs[e] = make_float2(sc, sc);
-    }
     __syncthreads();
     if (F16) {
-      for (int e = tid; e < nch * RP * KMAX; e += P::NT) {
-        const int tl = e / (RP * KMAX), r = (e / KMAX) % RP, sl = e % KMAX;
+      for (int e = tid; e < nch * RP; e += P::NT) {
+        const int tl = e / RP, r = e % RP;
         const int y2 = y2_0 + r;
         const TiltParams tp = s_tp[tl];
-        if (y2 < Y2 && sl < tp.nk) {
-          const size_t row = ((size_t)y2 * a.D + (tp.k0 + sl)) * a.T + (tbase + tl);
-          const float2 f = s_rs[e];
-          s_rs[e] = make_float2(f.x * __int_as_float((127 - a.row_exp[2 * row]) << 23),
-                                f.y * __int_as_float((127 - a.row_exp[2 * row + 1]) << 23));
+        int ea[KMAX], eb[KMAX];
+        int ra = 127, rb = 127;
+#pragma unroll
+        for (int sl = 0; sl < KMAX; ++sl) {
+          ea[sl] = eb[sl] = 127;
+          if (y2 < Y2 && sl < tp.nk) {
+            const size_t row = ((size_t)y2 * a.D + (tp.k0 + sl)) * a.T + (tbase + tl);
+            ea[sl] = a.row_exp[2 * row];
+            eb[sl] = a.row_exp[2 * row + 1];
+            ra = min(ra, ea[sl]);
+            rb = min(rb, eb[sl]);
+          }
         }
+        if (ra == 127) ra = rb = 0;  // no staged rows for this pair
+        const float sc = a.geom[tbase + tl].scale;
+        s_rs[e] = make_float2(sc * __int_as_float((127 - ra) << 23),
+                              sc * __int_as_float((127 - rb) << 23));
+#pragma unroll
+        for (int sl = 0; sl < KMAX; ++sl)
+          s_fac[e * KMAX + sl] = half_pow2_neg(ea[sl] == 127 ? 0 : ea[sl] - ra) |
+                                 (half_pow2_neg(eb[sl] == 127 ? 0 : eb[sl] - rb) << 16);
       }
       __syncthreads();
     }
@@ -309,7 +331,26 @@ k_bp_fast(BpArgs a) {
       if (warp == 0 && grp + 1 < ngroups)
         issue_copies(tg + G, min(G, nch - tg - G), tbase, b ^ 1);
       mbar_wait(&s_bar[b], (gg >> 1) & 1, a.err);
-      const unsigned char *buf = smem_raw + b * P::BUF;
+      unsigned char *buf = smem_raw + b * P::BUF;
+      if (F16) {
+        // bring every slab's records of a row pair to its reference exponent
+        // (exact powers of two), so a voxel's scale does not depend on its slab
+        for (int slot = warp; slot < ng * RP * KMAX; slot += P::NT / 32) {
+          const unsigned f = s_fac[(size_t)tg * RP * KMAX + slot];
+          if (f == kHalf2One) continue;
+          const __half2 fh = *(const __half2 *)&f;
+          uint2 *rec = (uint2 *)(buf + (size_t)slot * P::SLOT_BYTES);
+          for (int px = lane; px < P::NPX_MAX; px += 32) {
+            uint2 q = rec[px];
+            const __half2 v = __hmul2(*(const __half2 *)&q.x, fh);
+            const __half2 dv = __hmul2(*(const __half2 *)&q.y, fh);
+            q.x = *(const unsigned *)&v;
+            q.y = *(const unsigned *)&dv;
+            rec[px] = q;
+          }
+        }
+        __syncthreads();
+      }
       for (int gi = 0; gi < ng; ++gi) {
         const TiltParams tp = s_tp[tg + gi];
         float xc[A], zs[B];
@@ -317,105 +358,89 @@ k_bp_fast(BpArgs a) {
         for (int i = 0; i < A; ++i) xc[i] = __fmul_rn(xf[i], tp.cos_a);
 #pragma unroll
         for (int j = 0; j < B; ++j) zs[j] = __fmul_rn(zf[j], tp.sin_a);
-        // Slab of each voxel.  Within the tile k = k0 + #{m in [1, nk) :
-        // defocus >= k0 + m - 1/2}: the reference's clamp(floor(defocus + 1/2))
-        // with the floor replaced by exact comparisons.  The defocus is the
-        // reference's float expression, monotone in x and z, so the thread's
-        // extremes sit at two opposite corners of its voxel box.
-        float xs[A], zc[B];
-        int cl = 0;
-        bool uniform = true;
-        if (tp.nk > 1) {
-#pragma unroll
-          for (int i = 0; i < A; ++i) xs[i] = __fmul_rn(-xf[i], tp.sin_a);
-#pragma unroll
-          for (int j = 0; j < B; ++j) zc[j] = __fmul_rn(zf[j], tp.cos_a);
-          const float xsl = tp.sin_a > 0.f ? xs[A - 1] : xs[0];
-          const float xsh = tp.sin_a > 0.f ? xs[0] : xs[A - 1];
-          const float zcl = tp.cos_a > 0.f ? zc[B - 1] : zc[0];
-          const float zch = tp.cos_a > 0.f ? zc[0] : zc[B - 1];
-          const float dl = __fadd_rn(__fmul_rn(__fsub_rn(xsl, zcl), a.dscale), a.doffset);
-          const float dh = __fadd_rn(__fmul_rn(__fsub_rn(xsh, zch), a.dscale), a.doffset);
-          int ch = 0;
-#pragma unroll
-          for (int m = 1; m < KMAX; ++m) {
-            const float bnd = (float)(tp.k0 + m) - 0.5f;
-            cl += (m < tp.nk && dl >= bnd) ? 1 : 0;
-            ch += (m < tp.nk && dh >= bnd) ? 1 : 0;
-          }
-          const int lo = min(cl, ch);
-          uniform = lo == max(cl, ch);
-          cl = lo;
-        }
         const unsigned char *tbuf = buf + (size_t)gi * RP * KMAX * P::SLOT_BYTES;
-        const float2 *trs = s_rs + (size_t)(tg + gi) * RP * KMAX;
         // byte offset of pixel p of slot (r, s): (r * KMAX + s) * SLOT_BYTES + (p - p_s) * PB;
         // the magic-number bias of the float bits folds into the same
         // constant (unsigned arithmetic wraps modulo 2^32 and cancels exactly)
         const unsigned bias = (unsigned)(-tp.p_s * P::PB) - (unsigned)kMagicBits * P::PB;
-        const unsigned base_u = (unsigned)(cl * P::SLOT_BYTES) + bias;
         u64 rs[RP];
         if (F16) {
+          const float2 *trs = s_rs + (size_t)(tg + gi) * RP;
 #pragma unroll
           for (int rr = 0; rr < RP; ++rr) {
-            const float2 f = trs[rr * KMAX + cl];
+            const float2 f = trs[rr];
             rs[rr] = f2_pack(f.x, f.y);
           }
         } else {
 #pragma unroll
           for (int rr = 0; rr < RP; ++rr) rs[rr] = f2_pack(tp.scale, tp.scale);
         }
+        // Slab of each voxel, when the tile spans several: k = k0 + #{m in
+        // [1, nk) : defocus >= k0 + m - 1/2}, the reference's
+        // clamp(floor(defocus + 1/2)) with the floor replaced by exact
+        // comparisons on the reference's float defocus expression; without
+        // branches, so that all voxels' loads can be scheduled together.
+        auto voxels = [&](auto multi_slab) {
+          constexpr bool MS = decltype(multi_slab)::value;
+          float xs[A], zc[B], bnd[KMAX];
+          if (MS) {
 #pragma unroll
-        for (int i = 0; i < A; ++i) {
+            for (int i = 0; i < A; ++i) xs[i] = __fmul_rn(-xf[i], tp.sin_a);
 #pragma unroll
-          for (int j = 0; j < B; ++j) {
-            const float q = detector_coord(xc[i], zs[j], tp.off);
-            const float r = __fadd_rd(q, kMagic);
-            const float t = __fsub_rn(q, __fsub_rn(r, kMagic));
-            unsigned off = base_u;
-            int c = cl;
-            if (!uniform) {
-              const float d = __fadd_rn(__fmul_rn(__fsub_rn(xs[i], zc[j]), a.dscale), a.doffset);
-              c = 0;
+            for (int j = 0; j < B; ++j) zc[j] = __fmul_rn(zf[j], tp.cos_a);
 #pragma unroll
-              for (int m = 1; m < KMAX; ++m)
-                c += (m < tp.nk && d >= (float)(tp.k0 + m) - 0.5f) ? 1 : 0;
-              off = (unsigned)(c * P::SLOT_BYTES) + bias;
-            }
-            off += (unsigned)__float_as_int(r) * (unsigned)P::PB;
-            if (tp.edge) {
-              // the reference skips samples unless 0 <= floor <= N-2
-              const unsigned ind = (unsigned)(__float_as_int(r) - kMagicBits);
-              if (ind > (unsigned)(a.N - 2)) off = P::NPX_MAX * P::PB;
-            }
-            const unsigned char *p0 = tbuf + off;
-            if (F16) {
-              const __half2 t2 = __float2half2_rn(t);
+            for (int m = 1; m < KMAX; ++m)
+              bnd[m] = m < tp.nk ? (float)(tp.k0 + m) - 0.5f : __int_as_float(0x7f800000);
+          }
 #pragma unroll
-              for (int rr = 0; rr < RP; ++rr) {
-                const unsigned char *p = p0 + rr * KMAX * P::SLOT_BYTES;
-                const uint2 rec = *(const uint2 *)p;  // (v_a, v_b), (dv_a, dv_b)
-                const __half2 v0 = *(const __half2 *)&rec.x, dv = *(const __half2 *)&rec.y;
-                const float2 val = __half22float2(__hfma2(t2, dv, v0));
-                u64 sc = rs[rr];
-                if (!uniform) {
-                  const float2 f = trs[rr * KMAX + c];
-                  sc = f2_pack(f.x, f.y);
-                }
-                acc[i][j][rr] = f2_fma(f2_pack(val.x, val.y), sc, acc[i][j][rr]);
+          for (int i = 0; i < A; ++i) {
+#pragma unroll
+            for (int j = 0; j < B; ++j) {
+              const float q = detector_coord(xc[i], zs[j], tp.off);
+              const float r = __fadd_rd(q, kMagic);
+              const float t = __fsub_rn(q, __fsub_rn(r, kMagic));
+              unsigned off = bias + (unsigned)__float_as_int(r) * (unsigned)P::PB;
+              if (MS) {
+                const float d =
+                    __fadd_rn(__fmul_rn(__fsub_rn(xs[i], zc[j]), a.dscale), a.doffset);
+                int c = 0;
+#pragma unroll
+                for (int m = 1; m < KMAX; ++m) c += d >= bnd[m] ? 1 : 0;
+                off += (unsigned)(c * P::SLOT_BYTES);
               }
-            } else {
-              const u64 tt = f2_pack(t, t);
+              if (tp.edge) {
+                // the reference skips samples unless 0 <= floor <= N-2
+                const unsigned ind = (unsigned)(__float_as_int(r) - kMagicBits);
+                if (ind > (unsigned)(a.N - 2)) off = P::NPX_MAX * P::PB;
+              }
+              const unsigned char *p0 = tbuf + off;
+              if (F16) {
+                const __half2 t2 = __float2half2_rn(t);
 #pragma unroll
-              for (int rr = 0; rr < RP; ++rr) {
-                const unsigned char *p = p0 + rr * KMAX * P::SLOT_BYTES;
-                const u64 v0 = *(const u64 *)p, v1 = *(const u64 *)(p + 8);
-                const u64 val = f2_fma(tt, f2_sub(v1, v0), v0);
-                acc[i][j][rr] = f2_fma(val, rs[rr], acc[i][j][rr]);
+                for (int rr = 0; rr < RP; ++rr) {
+                  const unsigned char *p = p0 + rr * KMAX * P::SLOT_BYTES;
+                  const uint2 rec = *(const uint2 *)p;  // (v_a, v_b), (dv_a, dv_b)
+                  const __half2 v0 = *(const __half2 *)&rec.x, dv = *(const __half2 *)&rec.y;
+                  const float2 val = __half22float2(__hfma2(t2, dv, v0));
+                  acc[i][j][rr] = f2_fma(f2_pack(val.x, val.y), rs[rr], acc[i][j][rr]);
+                }
+              } else {
+                const u64 tt = f2_pack(t, t);
+#pragma unroll
+                for (int rr = 0; rr < RP; ++rr) {
+                  const unsigned char *p = p0 + rr * KMAX * P::SLOT_BYTES;
+                  const u64 v0 = *(const u64 *)p, v1 = *(const u64 *)(p + 8);
+                  const u64 val = f2_fma(tt, f2_sub(v1, v0), v0);
+                  acc[i][j][rr] = f2_fma(val, rs[rr], acc[i][j][rr]);
+                }
               }
             }
           }
-        }
+        };
+        if (tp.nk > 1)
+          voxels(std::true_type{});
+        else
+          voxels(std::false_type{});
       }
     }
   }
