@@ -7,6 +7,8 @@
   ``guanaco`` functions on the device path; ``reconstruct_ctf`` runs both in
   one device pass.
 * ``FbpPlan`` -- the whole-series plan over the C ABI (include/guanaco_gb300.h).
+* ``reconstruct_file`` / ``correct_file`` -- the MRC file entry points
+  (``guanaco_gb300.mrc`` reads and writes MRC2014 with FEI1 headers).
 * ``serve.Server`` -- the request server: many tilt series of mixed shapes at
   once, with continuous batching on one GPU.
 """
@@ -19,8 +21,10 @@ from .api import (  # noqa: F401
     get_ctf_array,
     get_defocus_steps,
     get_weights,
+    correct_file,
     reconstruct,
     reconstruct_ctf,
+    reconstruct_file,
 )
 from .fbp import FbpDesc, FbpPlan  # noqa: F401
 

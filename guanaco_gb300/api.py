@@ -169,10 +169,13 @@ def correct_projections(projections, centre=None, pixel_size=1, energy=None, def
         out = dc.cpu().numpy()
     finally:
         plan.close()
+    if isinstance(corrected_output, str):  # correct.py:96-113: a memory-mapped file
+        corrected_output = np.memmap(corrected_output, mode="w+", dtype="float32",
+                                     shape=out.shape)
     if corrected_output is not None:
         target = np.asarray(corrected_output).reshape(out.shape)
         target[...] = out
-        out = target
+        out = corrected_output.reshape(out.shape)
     if nd == 1:
         out = out.reshape(proj.shape)
     return out, mn - defocus, mx - defocus
@@ -249,3 +252,111 @@ def reconstruct_ctf(projections, angles, centre=None, pixel_size=1, energy=300, 
         return plan.execute_host(proj)
     finally:
         plan.close()
+
+
+# ------------------------------------------------------------------ MRC files
+def _read_projection_metadata(infile):
+    """Angles (rad, float32) from the FEI1 "Alpha tilt" records, the voxel size,
+    and for a corrected stack the relative defocus range from the "Defocus"
+    records (reconstruct.py:248-304)."""
+    from . import mrc
+
+    ang = mrc.fei1_angles_deg(infile)
+    assert infile.data.shape[0] == ang.shape[0], "Inconsistent data/header shape"
+    angles = np.deg2rad(ang).astype(np.float32)
+    if infile.data.ndim == 4:
+        df = mrc.fei1_defocus(infile).astype(np.float32)
+        assert infile.data.shape[1] == df.shape[0], "Inconsistent data/header shape"
+        return angles, infile.voxel_size, float(np.min(df)), float(np.max(df))
+    return angles, infile.voxel_size, 0, 0
+
+
+def reconstruct_file(input_filename, output_filename, corrected_filename="GUANACO_CORRECTED.dat",
+                     start_angle=None, step_angle=None, pixel_size=None, centre=None, energy=None,
+                     defocus=None, num_defocus=None, step_defocus=None, spherical_aberration=None,
+                     astigmatism=None, astigmatism_angle=None, phase_shift=None, device="cpu",
+                     ncore=None, transform=None, angular_weights=False, chunk_size=None,
+                     method="FBP_CTF", num_iter=None, staging="f32"):
+    """src/guanaco/detail/reconstruct.py:216-402 on the device.
+
+    Reads an MRC tilt series (T, H, W) -- or an already corrected stack
+    (T, D, H, W) -- with its angles (FEI1 "Alpha tilt") and voxel size unless
+    ``start_angle``, ``step_angle`` and ``pixel_size`` are all given, and writes
+    the (H, W, W) float32 volume with the same voxel size.  Raw projections
+    with a ``defocus`` are corrected and reconstructed in one device pass; the
+    corrected stack stays on the GPU, so ``corrected_filename`` is not written
+    (``correct_file`` writes it).  Only the FBP_CTF method is provided (the
+    reference hands the others to tomopy)."""
+    from . import mrc
+
+    _gpu(device)
+    if method != "FBP_CTF":
+        raise RuntimeError(f"reconstruct_file: method {method!r} is not provided here "
+                           "(only FBP_CTF; the reference delegates the others to tomopy)")
+    infile = mrc.open_mrc(input_filename)
+    projections = infile.data
+    if start_angle is None or step_angle is None or pixel_size is None:
+        angles, voxel_size, min_defocus, max_defocus = _read_projection_metadata(infile)
+        assert voxel_size["x"] == voxel_size["y"], "Pixel must be a square"
+        pixel_size = voxel_size["x"]
+        voxel = (voxel_size["x"], voxel_size["y"], voxel_size["z"])
+    else:
+        angles = np.deg2rad(start_angle + np.arange(projections.shape[0]) * step_angle)
+        angles = angles.astype(np.float32)
+        voxel = pixel_size
+        min_defocus = max_defocus = 0
+    H, W = projections.shape[-2], projections.shape[-1]
+    centre = get_centre(projections.shape, centre, False)
+    if projections.ndim == 4:
+        volume = reconstruct(np.asarray(projections), angles, None, centre, pixel_size,
+                             min_defocus, max_defocus, False, transform, angular_weights,
+                             device=device, staging=staging)
+    else:
+        volume = reconstruct_ctf(np.asarray(projections), angles, centre, pixel_size,
+                                 energy=energy, defocus=defocus, num_defocus=num_defocus,
+                                 step_defocus=step_defocus,
+                                 spherical_aberration=spherical_aberration or 0,
+                                 astigmatism=astigmatism or 0,
+                                 astigmatism_angle=astigmatism_angle or 0,
+                                 phase_shift=phase_shift or 0, transform=transform,
+                                 angular_weights=angular_weights, staging=staging,
+                                 device=device)
+    with mrc.new_mrc(output_filename, (H, W, W), np.float32, voxel) as outfile:
+        outfile.data[...] = volume
+    return volume
+
+
+def correct_file(input_filename, output_filename, centre=None, energy=None, defocus=None,
+                 num_defocus=None, step_defocus=None, spherical_aberration=None, astigmatism=None,
+                 astigmatism_angle=None, phase_shift=None, device="cpu"):
+    """src/guanaco/detail/correct.py:321-473 on the device: the corrected
+    stack (T, D, H, W) with FEI1 records carrying each image's tilt and
+    relative defocus."""
+    from . import mrc
+
+    _gpu(device)
+    infile = mrc.open_mrc(input_filename)
+    ang = mrc.fei1_angles_deg(infile)
+    assert infile.data.shape[0] == ang.shape[0], "Inconsistent data/header array shape"
+    angles = np.deg2rad(ang).astype(np.float32)
+    voxel_size = infile.voxel_size
+    assert voxel_size["x"] == voxel_size["y"]
+    pixel_size = voxel_size["x"]
+    projections = np.asarray(infile.data)
+    centre = get_centre(projections.shape, centre, False)
+    if num_defocus is None or num_defocus == 0:
+        num_defocus = 1
+        step_defocus = 0
+    shape = (projections.shape[0], num_defocus, projections.shape[1], projections.shape[2])
+    with mrc.new_mrc(output_filename, shape, np.float32,
+                     (voxel_size["x"], voxel_size["y"], voxel_size["z"]), fei1=True) as outfile:
+        _, min_defocus, max_defocus = correct_projections(
+            projections, centre, pixel_size, energy, defocus, num_defocus, step_defocus,
+            spherical_aberration or 0, astigmatism or 0, astigmatism_angle or 0,
+            phase_shift or 0, outfile.data, device)
+        if step_defocus is None:
+            step_defocus = 0 if num_defocus == 1 else (max_defocus - min_defocus) / (num_defocus - 1)
+        for j in range(shape[0]):
+            for i in range(shape[1]):
+                outfile.extended_header[j, i]["Alpha tilt"] = np.rad2deg(angles[j])
+                outfile.extended_header[j, i]["Defocus"] = min_defocus + i * step_defocus

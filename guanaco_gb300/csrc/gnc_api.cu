@@ -172,7 +172,11 @@ struct gnc_fbp_plan {
   SignTableArgs sargs{};
   // device memory
   float2 *spec = nullptr;   // (T, H, W/2)
-  float2 *gbuf = nullptr;   // (chunk, D, H, W/2)
+  float2 *gbuf = nullptr;   // 2 x (chunk, D, H, W/2): flips of two chunks in flight
+  // side stream for the phase flips, so a chunk's flip overlaps the previous
+  // chunk's row stage; events: fork, flip done (per buffer), rows done (per buffer)
+  cudaStream_t s_flip = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_flip[2] = {}, ev_rows[2] = {};
   void *staged = nullptr;   // (Y2, D, T, W) pairs
   int8_t *row_exp = nullptr;
   int8_t *sign = nullptr;   // (D, H, W/2 + 1)
@@ -197,6 +201,12 @@ struct gnc_fbp_plan {
 static void plan_free(gnc_fbp_plan *p) {
   cudaFree(p->spec);
   cudaFree(p->gbuf);
+  if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+  for (cudaEvent_t e : p->ev_flip)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : p->ev_rows)
+    if (e) cudaEventDestroy(e);
+  if (p->s_flip) cudaStreamDestroy(p->s_flip);
   cudaFree(p->staged);
   cudaFree(p->row_exp);
   cudaFree(p->sign);
@@ -328,7 +338,8 @@ size_t plan_bytes(const gnc_fbp_desc *d) {
   if (ctf) {
     const size_t per_tilt = D * H * half * sizeof(float2);
     const size_t chunk = std::max<size_t>(1, std::min<size_t>(T, (48ull << 20) / per_tilt));
-    b += T * H * half * sizeof(float2) + chunk * D * H * half * sizeof(float2) + D * H * (half + 1);
+    b += T * H * half * sizeof(float2) + 2 * chunk * D * H * half * sizeof(float2) +
+         D * H * (half + 1);
   }
   b += (Y2 * D * T * W + 8) * kStagedPixelBytes;
   if (d->staging == GNC_STAGE_F16) b += Y2 * D * T * 2;
@@ -427,7 +438,13 @@ int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
     size_t per_tilt = (size_t)p->D * p->H * half * sizeof(float2);
     p->chunk = (int)std::max<size_t>(1, std::min<size_t>(p->T, (48ull << 20) / per_tilt));
     if (e == cudaSuccess) e = dalloc(p, &p->spec, (size_t)p->T * p->H * half);
-    if (e == cudaSuccess) e = dalloc(p, &p->gbuf, (size_t)p->chunk * p->D * p->H * half);
+    if (e == cudaSuccess) e = dalloc(p, &p->gbuf, 2 * (size_t)p->chunk * p->D * p->H * half);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->s_flip, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming);
+    for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+      e = cudaEventCreateWithFlags(&p->ev_flip[b], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_rows[b], cudaEventDisableTiming);
+    }
     if (e == cudaSuccess) e = dalloc(p, &p->sign, (size_t)p->D * p->H * (half + 1));
   }
   // +8 pixels: a 16-byte aligned bulk copy of the last row may run past its end
@@ -465,6 +482,35 @@ int gnc_fbp_sign_table(gnc_fbp_plan *p, int8_t *d_out, void *stream) {
   return GNC_OK;
 }
 
+// Phase flip and row stage of the tilts [t_begin, t_end), chunk by chunk: the
+// flips run on the plan's side stream into two alternating buffers, so chunk
+// c + 1 is flipped while chunk c's rows are filtered on s.  out_rows (plain
+// corrected rows) or null (the row stage writes r's staged output).
+static int flip_rows(gnc_fbp_plan *p, RowStageArgs r, int t_begin, int t_end, float *out_rows,
+                     cudaStream_t s) {
+  const size_t gsz = (size_t)p->chunk * p->D * p->H * (p->W / 2);
+  // everything on s so far (spectra, sign table, earlier row stages) comes first
+  GNC_CUDA(cudaEventRecord(p->ev_fork, s));
+  GNC_CUDA(cudaStreamWaitEvent(p->s_flip, p->ev_fork, 0));
+  int k = 0;
+  for (int c0 = t_begin; c0 < t_end; c0 += p->chunk, ++k) {
+    const int nt = std::min(p->chunk, t_end - c0);
+    const int b = k & 1;
+    float2 *g = p->gbuf + b * gsz;
+    if (k >= 2) GNC_CUDA(cudaStreamWaitEvent(p->s_flip, p->ev_rows[b], 0));
+    GNC_CUDA(launch_column_flip(p->spec, g, p->sign, c0, nt, p->D, p->H, p->W, p->s_flip));
+    GNC_CUDA(cudaEventRecord(p->ev_flip[b], p->s_flip));
+    GNC_CUDA(cudaStreamWaitEvent(s, p->ev_flip[b], 0));
+    r.g = g;
+    r.nt = nt;
+    r.t0 = c0;
+    if (out_rows) r.out_rows = out_rows + (size_t)c0 * p->D * p->H * p->W;
+    GNC_CUDA(launch_row_stage(r, s));
+    GNC_CUDA(cudaEventRecord(p->ev_rows[b], s));
+  }
+  return GNC_OK;  // s has waited for every flip: the side stream is joined
+}
+
 // Raw or corrected input -> staged filtered rows (the plan's staging buffer).
 int gnc_fbp_stage(gnc_fbp_plan *p, const float *d_input, void *stream) {
   GNC_REQUIRE(p != nullptr && d_input != nullptr);
@@ -485,14 +531,8 @@ int gnc_fbp_stage(gnc_fbp_plan *p, const float *d_input, void *stream) {
     GNC_CUDA(launch_rfft_rows(d_input, p->spec, p->T, p->H, p->W, s));
     GNC_CUDA(launch_column_fft(p->spec, p->T, p->H, p->W, s));
     r.input_spectra = 1;
-    r.g = p->gbuf;
-    for (int t0 = 0; t0 < p->T; t0 += p->chunk) {
-      int nt = std::min(p->chunk, p->T - t0);
-      GNC_CUDA(launch_column_flip(p->spec, p->gbuf, p->sign, t0, nt, p->D, p->H, p->W, s));
-      r.nt = nt;
-      r.t0 = t0;
-      GNC_CUDA(launch_row_stage(r, s));
-    }
+    const int st = flip_rows(p, r, 0, p->T, nullptr, s);
+    if (st != GNC_OK) return st;
   } else {
     r.input_spectra = 0;
     r.rows = d_input;
@@ -584,7 +624,6 @@ static int execute_host_pipelined(gnc_fbp_plan *p, const float *h_input, float *
   if (p->correct) {
     GNC_CUDA(launch_sign_table(p->sargs, p->sign, s));
     r.input_spectra = 1;
-    r.g = p->gbuf;
   } else {
     r.input_spectra = 0;
     r.rows = p->io_in;
@@ -599,13 +638,8 @@ static int execute_host_pipelined(gnc_fbp_plan *p, const float *h_input, float *
       float2 *spec = p->spec + (size_t)t0 * p->H * half;
       GNC_CUDA(launch_rfft_rows(p->io_in + (size_t)t0 * per_tilt, spec, n, p->H, p->W, s));
       GNC_CUDA(launch_column_fft(spec, n, p->H, p->W, s));
-      for (int c0 = t0; c0 < t0 + n; c0 += p->chunk) {
-        const int nt = std::min(p->chunk, t0 + n - c0);
-        GNC_CUDA(launch_column_flip(p->spec, p->gbuf, p->sign, c0, nt, p->D, p->H, p->W, s));
-        r.nt = nt;
-        r.t0 = c0;
-        GNC_CUDA(launch_row_stage(r, s));
-      }
+      const int st = flip_rows(p, r, t0, t0 + n, nullptr, s);
+      if (st != GNC_OK) return st;
     } else {
       r.nt = n;
       r.t0 = t0;
@@ -663,22 +697,13 @@ int gnc_fbp_correct(gnc_fbp_plan *p, const float *d_proj, float *d_corrected, vo
   GNC_CUDA(launch_column_fft(p->spec, p->T, p->H, p->W, s));
   RowStageArgs r{};
   r.input_spectra = 1;
-  r.g = p->gbuf;
   r.D = p->D;
   r.H = p->H;
   r.N = p->W;
   r.T = p->T;
   r.ramp = 0;
   r.out_staged = 0;
-  for (int t0 = 0; t0 < p->T; t0 += p->chunk) {
-    int nt = std::min(p->chunk, p->T - t0);
-    GNC_CUDA(launch_column_flip(p->spec, p->gbuf, p->sign, t0, nt, p->D, p->H, p->W, s));
-    r.nt = nt;
-    r.t0 = t0;
-    r.out_rows = d_corrected + (size_t)t0 * p->D * p->H * p->W;
-    GNC_CUDA(launch_row_stage(r, s));
-  }
-  return GNC_OK;
+  return flip_rows(p, r, 0, p->T, d_corrected, s);
 }
 
 int gnc_fbp_slab_map(gnc_fbp_plan *p, int32_t *d_out, void *stream) {

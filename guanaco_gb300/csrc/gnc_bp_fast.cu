@@ -322,35 +322,41 @@ k_bp_fast(BpArgs a) {
       __syncthreads();
     }
     const int ngroups = (nch + G - 1) / G;
+    // FP16: once group g has landed in buffer b, bring every slab's records of
+    // a row pair to its reference exponent (exact powers of two), so a voxel's
+    // scale does not depend on its slab.  Done for group g + 1 at the end of
+    // group g, so the group's barrier also covers it.
+    auto land = [&](int grp_l, int gg_l) {
+      mbar_wait(&s_bar[gg_l & 1], (gg_l >> 1) & 1, a.err);
+      if (!F16) return;
+      unsigned char *lb = smem_raw + (gg_l & 1) * P::BUF;
+      const int tg_l = grp_l * G, ng_l = min(G, nch - tg_l);
+      for (int slot = warp; slot < ng_l * RP * KMAX; slot += P::NT / 32) {
+        const unsigned f = s_fac[(size_t)tg_l * RP * KMAX + slot];
+        if (f == kHalf2One) continue;
+        const __half2 fh = *(const __half2 *)&f;
+        uint2 *rec = (uint2 *)(lb + (size_t)slot * P::SLOT_BYTES);
+        for (int px = lane; px < P::NPX_MAX; px += 32) {
+          uint2 q = rec[px];
+          const __half2 v = __hmul2(*(const __half2 *)&q.x, fh);
+          const __half2 dv = __hmul2(*(const __half2 *)&q.y, fh);
+          q.x = *(const unsigned *)&v;
+          q.y = *(const unsigned *)&dv;
+          rec[px] = q;
+        }
+      }
+    };
     if (warp == 0) issue_copies(0, min(G, nch), tbase, gg & 1);
+    if (F16) land(0, gg);
     for (int grp = 0; grp < ngroups; ++grp, ++gg) {
       const int b = gg & 1;
       const int tg = grp * G;  // within the chunk
       const int ng = min(G, nch - tg);
-      __syncthreads();  // everyone is done with buffer b^1
+      __syncthreads();  // buffer b^1 is free; buffer b has landed (FP16: rescaled)
       if (warp == 0 && grp + 1 < ngroups)
         issue_copies(tg + G, min(G, nch - tg - G), tbase, b ^ 1);
-      mbar_wait(&s_bar[b], (gg >> 1) & 1, a.err);
-      unsigned char *buf = smem_raw + b * P::BUF;
-      if (F16) {
-        // bring every slab's records of a row pair to its reference exponent
-        // (exact powers of two), so a voxel's scale does not depend on its slab
-        for (int slot = warp; slot < ng * RP * KMAX; slot += P::NT / 32) {
-          const unsigned f = s_fac[(size_t)tg * RP * KMAX + slot];
-          if (f == kHalf2One) continue;
-          const __half2 fh = *(const __half2 *)&f;
-          uint2 *rec = (uint2 *)(buf + (size_t)slot * P::SLOT_BYTES);
-          for (int px = lane; px < P::NPX_MAX; px += 32) {
-            uint2 q = rec[px];
-            const __half2 v = __hmul2(*(const __half2 *)&q.x, fh);
-            const __half2 dv = __hmul2(*(const __half2 *)&q.y, fh);
-            q.x = *(const unsigned *)&v;
-            q.y = *(const unsigned *)&dv;
-            rec[px] = q;
-          }
-        }
-        __syncthreads();
-      }
+      if (!F16) land(grp, gg);
+      const unsigned char *buf = smem_raw + b * P::BUF;
       for (int gi = 0; gi < ng; ++gi) {
         const TiltParams tp = s_tp[tg + gi];
         float xc[A], zs[B];
@@ -442,6 +448,7 @@ k_bp_fast(BpArgs a) {
         else
           voxels(std::false_type{});
       }
+      if (F16 && grp + 1 < ngroups) land(grp + 1, gg + 1);
     }
   }
   // ---- store
