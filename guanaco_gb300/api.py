@@ -163,7 +163,7 @@ def correct_projections(projections, centre=None, pixel_size=1, energy=None, def
                    spherical_aberration=spherical_aberration, astigmatism=astigmatism,
                    astigmatism_angle=astigmatism_angle, phase_shift=phase_shift)
     try:
-        dp = torch.from_numpy(proj).cuda()
+        dp = torch.from_numpy(np.require(proj, np.float32, ["C", "W"])).cuda()
         dc = torch.empty((T, nd, H, W), dtype=torch.float32, device="cuda")
         plan.correct(dp, dc)
         out = dc.cpu().numpy()
