@@ -92,15 +92,26 @@ __global__ void __launch_bounds__(256) k_rfft_rows_p2(const float *__restrict__ 
 // FLIP: per-slab phase flip before an inverse transform (see gnc_correct.cu
 // for the packed DC/Nyquist column).
 // ---------------------------------------------------------------------------
+// Columns per block: 256 threads for short columns; tall columns (2048,
+// 4096) take 1024 threads so that a block still reads 32 or 64 contiguous
+// bytes of every row (four or eight columns).
+template <int H>
+struct ColTile {
+  static constexpr int NT = Pow2<H>::NT;
+  static constexpr int THREADS = H >= 2048 ? 1024 : 256;
+  static constexpr int C = THREADS / NT;
+  static constexpr size_t SMEM = (size_t)C * Pow2<H>::PADDED * sizeof(float2);
+};
+
 template <int H, bool FLIP>
-__global__ void __launch_bounds__(256) k_column_p2(const float2 *__restrict__ src,
-                                                   float2 *__restrict__ dst,
-                                                   const int8_t *__restrict__ sign, int t0,
-                                                   int D, int W,
-                                                   const float2 *__restrict__ roots) {
+__global__ void __launch_bounds__(ColTile<H>::THREADS) k_column_p2(
+    const float2 *__restrict__ src, float2 *__restrict__ dst, const int8_t *__restrict__ sign,
+    int t0, int D, int W, const float2 *__restrict__ roots) {
   using P = Pow2<H>;
-  constexpr int C = 256 / P::NT;
-  __shared__ float2 buf[C][P::PADDED];
+  constexpr int C = ColTile<H>::C;
+  constexpr int NTH = ColTile<H>::THREADS;
+  extern __shared__ float2 smem_col[];
+  float2(*buf)[P::PADDED] = reinterpret_cast<float2(*)[P::PADDED]>(smem_col);
   const int g = threadIdx.x / P::NT, j = threadIdx.x % P::NT;
   const int half = W / 2;
   const int c0 = blockIdx.x * C;
@@ -110,7 +121,7 @@ __global__ void __launch_bounds__(256) k_column_p2(const float2 *__restrict__ sr
   const float2 *F = src + (size_t)t * H * half;
   const int sw = half + 1;
   const int8_t *sg = FLIP ? sign + (size_t)d * H * sw : nullptr;
-  for (int i = threadIdx.x; i < H * C; i += 256) {
+  for (int i = threadIdx.x; i < H * C; i += NTH) {
     const int ky = i / C, c = i % C;
     const int kx = c0 + c;
     float2 r = make_float2(0.f, 0.f);
@@ -134,7 +145,7 @@ __global__ void __launch_bounds__(256) k_column_p2(const float2 *__restrict__ sr
   __syncthreads();
   fft_pow2<H, FLIP>(buf[g], j, roots, BlockSync());
   float2 *out = FLIP ? dst + ((size_t)tl * D + d) * H * half : dst + (size_t)t * H * half;
-  for (int i = threadIdx.x; i < H * C; i += 256) {
+  for (int i = threadIdx.x; i < H * C; i += NTH) {
     const int ky = i / C, c = i % C;
     const int kx = c0 + c;
     if (kx < half) out[(size_t)ky * half + kx] = buf[c][fpad(ky)];
@@ -362,10 +373,16 @@ static cudaError_t column_p2(const float2 *src, float2 *dst, const int8_t *sign,
                              int D, int W, cudaStream_t s) {
   FftPlan p;
   if (!make_fft_plan(H, &p)) return cudaErrorInvalidValue;
-  constexpr int C = 256 / Pow2<H>::NT;
+  using CT = ColTile<H>;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_column_p2<H, FLIP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)CT::SMEM);
+    attr = true;
+  }
   const int half = W / 2;
-  dim3 grid((half + C - 1) / C, FLIP ? D : 1, nt);
-  k_column_p2<H, FLIP><<<grid, 256, 0, s>>>(src, dst, sign, t0, D, W, p.roots);
+  dim3 grid((half + CT::C - 1) / CT::C, FLIP ? D : 1, nt);
+  k_column_p2<H, FLIP><<<grid, CT::THREADS, CT::SMEM, s>>>(src, dst, sign, t0, D, W, p.roots);
   return cudaGetLastError();
 }
 

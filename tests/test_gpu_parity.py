@@ -365,7 +365,8 @@ def test_linearity_at_full_detector_width(torch, oracle):
 # ------------------------------------------- power-of-two transform lengths
 @pytest.mark.parametrize("staging", ["f32", "f16"])
 @pytest.mark.parametrize("shape", [(5, 256, 1024, 48, 3), (7, 512, 256, 64, 4),
-                                   (3, 1024, 256, 32, 2), (6, 243, 512, 40, 5)])
+                                   (3, 1024, 256, 32, 2), (6, 243, 512, 40, 5),
+                                   (3, 2048, 256, 16, 2), (2, 4096, 128, 16, 3)])
 def test_pipeline_pow2_sizes_vs_oracles(torch, oracle, staging, shape):
     T, H, W, Z, D = shape
     plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=T, H=H, W=W, Z=Z, D=D, staging=staging,
