@@ -134,8 +134,13 @@ using namespace gnc;
 
 // ------------------------------------------------------------- the plan ----
 // Host-buffer pipeline: input copies in up to kIoGroups tilt groups, volume
-// copies out in up to kIoSlabs row slabs, plus two events for the stream joins.
-constexpr int kIoGroups = 32, kIoSlabs = 8, kIoEvents = kIoGroups + kIoSlabs + 2;
+// copies out in up to kIoSlabs row slabs (eight, the last one split in three
+// so the copy that remains after the last kernel is short), plus two events
+// for the stream joins.
+constexpr int kIoGroups = 32, kIoSlabs = 10, kIoEvents = kIoGroups + kIoSlabs + 2;
+// Largest phase-flipped spectrum stack (T, D, H, W/2) the host-buffer path
+// keeps whole so that it can filter and backproject row slab by row slab.
+constexpr size_t kSlabMajorMaxBytes = (size_t)8 << 30;
 
 // Per-request parameter block of a plan: the same byte layout on the host and
 // on the device, so one copy moves all of it.
@@ -194,6 +199,8 @@ struct gnc_fbp_plan {
   size_t bytes = 0;
   // host-buffer path (gnc_fbp_execute_host), created on its first call
   float *io_in = nullptr, *io_out = nullptr;
+  float2 *gfull = nullptr;  // (T, D, H, W/2) flipped spectra (slab-major order)
+  bool gfull_tried = false;
   cudaStream_t s_in = nullptr, s_out = nullptr;
   cudaEvent_t ev[kIoEvents] = {};
 };
@@ -214,6 +221,7 @@ static void plan_free(gnc_fbp_plan *p) {
   cudaFree(p->err);
   cudaFree(p->io_in);
   cudaFree(p->io_out);
+  cudaFree(p->gfull);
   for (cudaEvent_t e : p->ev)
     if (e) cudaEventDestroy(e);
   if (p->s_in) cudaStreamDestroy(p->s_in);
@@ -593,12 +601,29 @@ static cudaError_t io_setup(gnc_fbp_plan *p, size_t in_elems, size_t out_elems) 
   return e;
 }
 
+// Host-buffer execution.  The input goes up in tilt groups on s_in and each
+// group's transforms start on arrival; the volume comes down in row slabs on
+// s_out while the next slab is computed.  With CTF correction and room for the
+// whole flipped stack, the phase flips of every tilt run first and the ramp
+// filter then runs slab by slab just ahead of that slab's backprojection, so
+// the first slab's copy-out starts after one slab of filtering instead of
+// after all of it.  Otherwise every tilt is filtered before the first slab.
 static int execute_host_pipelined(gnc_fbp_plan *p, const float *h_input, float *h_volume,
                                   cudaStream_t s) {
   const size_t per_tilt = (size_t)(p->input == GNC_INPUT_CORRECTED ? p->D : 1) * p->H * p->W;
   const size_t plane = (size_t)p->Z * p->X;
+  const size_t half = p->W / 2;
   cudaEvent_t *ev_in = p->ev, *ev_bp = p->ev + kIoGroups;
   cudaEvent_t ev_start = p->ev[kIoEvents - 2], ev_done = p->ev[kIoEvents - 1];
+  const size_t gfull_bytes = (size_t)p->T * p->D * p->H * half * sizeof(float2);
+  if (p->correct && !p->gfull && !p->gfull_tried && gfull_bytes <= kSlabMajorMaxBytes) {
+    p->gfull_tried = true;
+    if (cudaMalloc((void **)&p->gfull, gfull_bytes) != cudaSuccess) {
+      p->gfull = nullptr;
+      (void)cudaGetLastError();  // not enough memory: filter every tilt first instead
+    }
+  }
+  const bool slab_major = p->correct && p->gfull != nullptr;
   // the previous call's reads of the I/O buffers are ordered before this one
   GNC_CUDA(cudaEventRecord(ev_start, s));
   GNC_CUDA(cudaStreamWaitEvent(p->s_in, ev_start, 0));
@@ -630,7 +655,6 @@ static int execute_host_pipelined(gnc_fbp_plan *p, const float *h_input, float *
     r.row_stride = p->W;
     r.plane_stride = (long)p->H * p->W;
   }
-  const size_t half = p->W / 2;
   for (int g = 0, t0 = 0; t0 < p->T; ++g, t0 += group) {
     const int n = std::min(group, p->T - t0);
     GNC_CUDA(cudaStreamWaitEvent(s, ev_in[g], 0));
@@ -638,19 +662,44 @@ static int execute_host_pipelined(gnc_fbp_plan *p, const float *h_input, float *
       float2 *spec = p->spec + (size_t)t0 * p->H * half;
       GNC_CUDA(launch_rfft_rows(p->io_in + (size_t)t0 * per_tilt, spec, n, p->H, p->W, s));
       GNC_CUDA(launch_column_fft(spec, n, p->H, p->W, s));
-      const int st = flip_rows(p, r, t0, t0 + n, nullptr, s);
-      if (st != GNC_OK) return st;
+      if (slab_major) {
+        GNC_CUDA(launch_column_flip(p->spec, p->gfull + (size_t)t0 * p->D * p->H * half, p->sign,
+                                    t0, n, p->D, p->H, p->W, s));
+      } else {
+        const int st = flip_rows(p, r, t0, t0 + n, nullptr, s);
+        if (st != GNC_OK) return st;
+      }
     } else {
       r.nt = n;
       r.t0 = t0;
       GNC_CUDA(launch_row_stage(r, s));
     }
   }
-  // backprojection in slabs of whole row pairs, each copied out when done
-  const int rows = ((p->H + 7) / 8 + 7) / 8 * 8;  // at most 8 slabs of whole block rows
+  if (slab_major) {
+    r.g = p->gfull;
+    r.t0 = 0;
+    r.nt = p->T;
+  }
+  // backprojection in slabs of whole row pairs, each copied out when done: at
+  // most 8 slabs of whole block rows, the last one split into 1/2, 1/4, 1/4
+  const int rows = ((p->H + 7) / 8 + 7) / 8 * 8;
+  int slab_y0[kIoSlabs + 1], nslab = 0;
+  for (int y0 = 0; y0 < p->H; y0 += rows) slab_y0[nslab++] = y0;
+  if (rows >= 32) {
+    const int last = slab_y0[nslab - 1], n_last = p->H - last;
+    const int a = std::min(rows / 2, n_last), b = std::min(rows / 4, n_last - a);
+    if (a < n_last) slab_y0[nslab++] = last + a;
+    if (b > 0 && a + b < n_last) slab_y0[nslab++] = last + a + b;
+  }
+  slab_y0[nslab] = p->H;
   const size_t pb = kStagedPixelBytes;
-  for (int j = 0, y0 = 0; y0 < p->H; ++j, y0 += rows) {
-    const int ny = std::min(rows, p->H - y0);
+  for (int j = 0; j < nslab; ++j) {
+    const int y0 = slab_y0[j], ny = slab_y0[j + 1] - y0;
+    if (slab_major) {  // the ramp filter of this slab's rows, every tilt and slab
+      r.y2_begin = y0 / 2;
+      r.y2_count = (ny + 1) / 2;
+      GNC_CUDA(launch_row_stage(r, s));
+    }
     BpArgs a = bp_args(p, p->io_out + (size_t)y0 * plane);
     const size_t pair0 = (size_t)(y0 / 2) * p->D * p->T;
     a.Y = ny;

@@ -103,6 +103,8 @@ struct RowStageArgs {
   int nt, D, H, N;       // tilts in this launch, slabs, rows per image, row length
   int t0;                // first tilt of this launch (into weights/output)
   int T;                 // total tilts (output layout)
+  int y2_begin;          // first row pair of this launch
+  int y2_count;          // row pairs in this launch; 0: all (H + 1) / 2
   int ramp;              // apply the ramp filter
   // per-tilt factor (weight * sign) or null
   const float *tilt_factor;
@@ -114,6 +116,10 @@ struct RowStageArgs {
   float *out_rows;       // plain rows: (nt, D, H, N) at [t][d][y][n]
 };
 cudaError_t launch_row_stage(const RowStageArgs &a, cudaStream_t s);
+// Row pairs a row-stage launch covers: rows 2 y2_begin .. of every (tilt, slab).
+__host__ __device__ inline int row_pairs(const RowStageArgs &a) {
+  return a.y2_count > 0 ? a.y2_count : (a.H + 1) / 2;
+}
 
 // Backprojection of the staged pairs into the volume (Y, Z, X).
 struct BpArgs {

@@ -167,14 +167,14 @@ __global__ void __launch_bounds__(256) k_row_p2(RowStageArgs a, const float2 *__
   const int g = threadIdx.x / P::NT, j = threadIdx.x % P::NT;
   float2 *zb = smem_p2 + (size_t)(g * NB) * P::PADDED;  // c, then the odd path
   float2 *eb = zb + P::PADDED;                          // the even path
-  const int Y2 = (a.H + 1) / 2;
+  const int Y2 = row_pairs(a);  // row pairs of this launch
   const long npairs = (long)a.nt * a.D * Y2;
   long pair = (long)blockIdx.x * GPB + g;
   const bool active = pair < npairs;
   if (!active) pair = npairs - 1;
   const int tl = (int)(pair / ((long)a.D * Y2));
   const int rem = (int)(pair - (long)tl * a.D * Y2);
-  const int d = rem / Y2, y2 = rem - d * Y2;
+  const int d = rem / Y2, y2 = a.y2_begin + (rem - d * Y2);
   const int t = a.t0 + tl;
   const int ya = 2 * y2;
   const bool hb = ya + 1 < a.H;
@@ -422,7 +422,7 @@ static cudaError_t row_p2(const RowStageArgs &a, cudaStream_t s) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr = true;
   }
-  const long npairs = (long)a.nt * a.D * ((a.H + 1) / 2);
+  const long npairs = (long)a.nt * a.D * row_pairs(a);
   kern<<<(unsigned)((npairs + GPB - 1) / GPB), 256, smem, s>>>(a, pN.roots, p2N.roots);
   return cudaGetLastError();
 }

@@ -20,7 +20,7 @@ __global__ void k_row_stage(RowStageArgs a, FftPlan planN, FftPlan plan2N, int r
   __shared__ unsigned int s_max[2 * 8];
   const int N = a.N;
   const int L = RAMP ? 2 * N : N;
-  const int Y2 = (a.H + 1) / 2;
+  const int Y2 = row_pairs(a);  // row pairs of this launch
   const long npairs = (long)a.nt * a.D * Y2;
   const long P0 = (long)blockIdx.x * rp;
   const int np = (int)min((long)rp, npairs - P0);
@@ -35,7 +35,7 @@ __global__ void k_row_stage(RowStageArgs a, FftPlan planN, FftPlan plan2N, int r
       long P = P0 + s;
       int tl = (int)(P / ((long)a.D * Y2));
       int rem = (int)(P - (long)tl * a.D * Y2);
-      int d = rem / Y2, y2 = rem - d * Y2;
+      int d = rem / Y2, y2 = a.y2_begin + (rem - d * Y2);
       int ya = 2 * y2;
       bool hb = ya + 1 < a.H;
       if (SPECTRA) {
@@ -100,7 +100,7 @@ __global__ void k_row_stage(RowStageArgs a, FftPlan planN, FftPlan plan2N, int r
     long P = P0 + s;
     int tl = (int)(P / ((long)a.D * Y2));
     int rem = (int)(P - (long)tl * a.D * Y2);
-    int d = rem / Y2, y2 = rem - d * Y2;
+    int d = rem / Y2, y2 = a.y2_begin + (rem - d * Y2);
     int t = a.t0 + tl;
     int ya = 2 * y2;
     bool hb = ya + 1 < a.H;
@@ -172,7 +172,7 @@ static cudaError_t launch_variant(const RowStageArgs &a, cudaStream_t s) {
   if (RAMP && !make_fft_plan(2 * N, &p2N)) return cudaErrorInvalidValue;
   int rp = L >= 4096 ? 1 : 4096 / L;
   if (rp > 8) rp = 8;
-  const long npairs = (long)a.nt * a.D * ((a.H + 1) / 2);
+  const long npairs = (long)a.nt * a.D * row_pairs(a);
   if (rp > npairs) rp = (int)npairs;
   if (rp < 1) rp = 1;
   size_t smem = 2ull * rp * L * sizeof(float2);

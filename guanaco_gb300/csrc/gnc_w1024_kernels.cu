@@ -164,13 +164,13 @@ __global__ void __launch_bounds__(128, 3) k_row_w1024(RowStageArgs a,
   float2 *vb = tb + kWarpFftSlots;                           // parking slots
   warp_fft_twiddles(tw, roots);
   __syncthreads();
-  const int Y2 = (a.H + 1) / 2;
+  const int Y2 = row_pairs(a);  // row pairs of this launch
   const long npairs = (long)a.nt * a.D * Y2;
   const long pair = (long)blockIdx.x * WPB + w;
   if (pair >= npairs) return;
   const int tl = (int)(pair / ((long)a.D * Y2));
   const int rem = (int)(pair - (long)tl * a.D * Y2);
-  const int d = rem / Y2, y2 = rem - d * Y2;
+  const int d = rem / Y2, y2 = a.y2_begin + (rem - d * Y2);
   const int t = a.t0 + tl;
   const int ya = 2 * y2;
   const bool hb = ya + 1 < a.H;
@@ -395,7 +395,7 @@ static cudaError_t row_w1024(const RowStageArgs &a, cudaStream_t s) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr = true;
   }
-  const long npairs = (long)a.nt * a.D * ((a.H + 1) / 2);
+  const long npairs = (long)a.nt * a.D * row_pairs(a);
   kern<<<(unsigned)((npairs + 3) / 4), 128, smem, s>>>(a, roots, roots2N);
   return cudaGetLastError();
 }
