@@ -174,6 +174,12 @@ cudaError_t launch_column_fft_w1024(float2 *spec, int T, int W, cudaStream_t s);
 cudaError_t launch_column_flip_w1024(const float2 *spec, float2 *g, const int8_t *sign, int t0,
                                      int nt, int D, int W, cudaStream_t s);
 cudaError_t launch_row_stage_w1024(const RowStageArgs &a, cudaStream_t s);
+// Block-transform kernels for 4096-pixel columns and rows
+// (gnc_b4096_kernels.cu); the launchers above prefer them for that size.
+cudaError_t launch_column_fft_b4096(float2 *spec, int T, int W, cudaStream_t s);
+cudaError_t launch_column_flip_b4096(const float2 *spec, float2 *g, const int8_t *sign, int t0,
+                                     int nt, int D, int W, cudaStream_t s);
+cudaError_t launch_row_stage_b4096(const RowStageArgs &a, cudaStream_t s);
 
 // Exact slab index of the reference (reconstructor.cpp:66-72): the height and
 // defocus coordinate in float without contraction, then

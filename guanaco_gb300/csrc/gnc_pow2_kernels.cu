@@ -1,7 +1,9 @@
-// Correction and ramp-filter kernels for power-of-two sizes (256 .. 4096),
-// built on the register-resident FFT of gnc_fft_pow2.cuh.  Same results as
-// the generic kernels of gnc_correct.cu / gnc_ramp.cu (up to float rounding),
-// which keep serving every other size.
+// Correction and ramp-filter kernels for power-of-two sizes (256 .. 4096; the
+// column and row stages of 1024 and 4096 use the kernels of
+// gnc_w1024_kernels.cu and gnc_b4096_kernels.cu), built on the shared-memory
+// FFT of gnc_fft_pow2.cuh.  Same results as the generic kernels of
+// gnc_correct.cu / gnc_ramp.cu (up to float rounding), which keep serving
+// every other size.
 //
 // Ramp filter without 2N-point transforms.  For a row c of N samples (two
 // real rows packed as one complex row) the reference zero pads to 2N,
@@ -92,8 +94,8 @@ __global__ void __launch_bounds__(256) k_rfft_rows_p2(const float *__restrict__ 
 // FLIP: per-slab phase flip before an inverse transform (see gnc_correct.cu
 // for the packed DC/Nyquist column).
 // ---------------------------------------------------------------------------
-// Columns per block: 256 threads for short columns; tall columns (2048,
-// 4096) take 1024 threads so that a block still reads 32 or 64 contiguous
+// Columns per block: 256 threads for short columns; tall columns (2048)
+// take 1024 threads so that a block still reads 32 or 64 contiguous
 // bytes of every row (four or eight columns).
 template <int H>
 struct ColTile {
@@ -392,7 +394,6 @@ cudaError_t launch_column_fft_p2(float2 *spec, int T, int H, int W, cudaStream_t
     case 512: return column_p2<512, false>(spec, spec, nullptr, 0, T, 1, W, s);
     case 1024: return column_p2<1024, false>(spec, spec, nullptr, 0, T, 1, W, s);
     case 2048: return column_p2<2048, false>(spec, spec, nullptr, 0, T, 1, W, s);
-    case 4096: return column_p2<4096, false>(spec, spec, nullptr, 0, T, 1, W, s);
   }
   return cudaErrorInvalidValue;
 }
@@ -404,7 +405,6 @@ cudaError_t launch_column_flip_p2(const float2 *spec, float2 *g, const int8_t *s
     case 512: return column_p2<512, true>(spec, g, sign, t0, nt, D, W, s);
     case 1024: return column_p2<1024, true>(spec, g, sign, t0, nt, D, W, s);
     case 2048: return column_p2<2048, true>(spec, g, sign, t0, nt, D, W, s);
-    case 4096: return column_p2<4096, true>(spec, g, sign, t0, nt, D, W, s);
   }
   return cudaErrorInvalidValue;
 }
@@ -446,7 +446,6 @@ cudaError_t launch_row_stage_p2(const RowStageArgs &a, cudaStream_t s) {
     case 512: return row_p2_dispatch<512>(a, s);
     case 1024: return row_p2_dispatch<1024>(a, s);
     case 2048: return row_p2_dispatch<2048>(a, s);
-    case 4096: return row_p2_dispatch<4096>(a, s);
   }
   return cudaErrorInvalidValue;
 }

@@ -371,7 +371,8 @@ def test_linearity_at_full_detector_width(torch, oracle):
 @pytest.mark.parametrize("staging", ["f32", "f16"])
 @pytest.mark.parametrize("shape", [(5, 256, 1024, 48, 3), (7, 512, 256, 64, 4),
                                    (3, 1024, 256, 32, 2), (6, 243, 512, 40, 5),
-                                   (3, 2048, 256, 16, 2), (2, 4096, 128, 16, 3)])
+                                   (3, 2048, 256, 16, 2), (2, 4096, 128, 16, 3),
+                                   (2, 16, 4096, 16, 3)])
 def test_pipeline_pow2_sizes_vs_oracles(torch, oracle, staging, shape):
     T, H, W, Z, D = shape
     plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=T, H=H, W=W, Z=Z, D=D, staging=staging,
@@ -386,7 +387,7 @@ def test_pipeline_pow2_sizes_vs_oracles(torch, oracle, staging, shape):
         assert rel_l2(vol, ref) < FP16_TOL
 
 
-@pytest.mark.parametrize("W", [256, 512, 2048])
+@pytest.mark.parametrize("W", [256, 512, 2048, 4096])
 def test_plain_filter_pow2_vs_oracle(torch, oracle, W):
     """No CTF: the projections are ramp filtered and backprojected directly."""
     import guanaco_gb300 as G
@@ -408,8 +409,9 @@ def test_plain_filter_pow2_vs_oracle(torch, oracle, W):
     assert rel_l2(buf.cpu().numpy(), oracle.ramp_filter(rows)) < 1e-6
 
 
-def test_correct_only_pow2(torch, oracle):
-    plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=3, H=256, W=512, D=4, seed=4)
+@pytest.mark.parametrize("T,H,W,D", [(3, 256, 512, 4), (2, 16, 4096, 3), (1, 4096, 64, 2)])
+def test_correct_only_pow2(torch, oracle, T, H, W, D):
+    plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=T, H=H, W=W, D=D, seed=4)
     out = torch.empty((plan.T, plan.D, plan.H, plan.W), dtype=torch.float32, device="cuda")
     plan.correct(dev(torch, proj), out)
     got = out.cpu().numpy()
