@@ -555,11 +555,13 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the oracle parity/CPU sample")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving stream")
-    ap.add_argument("--case", choices=["3dctf", "profile", "large"], default="3dctf",
+    ap.add_argument("--case", choices=["3dctf", "profile", "large", "large_profile"],
+                    default="3dctf",
                     help="profile: the same 1024^2 ndf=10 kernels on 16 tilts and a 64-voxel-"
                          "thick volume, small enough for ncu captures (not a bench line); "
                          "large: 4096^2 projections, ndf=20, 4096x4096x512 volume in one "
-                         "HBM pass")
+                         "HBM pass; large_profile: the 4096^2 kernels on 2 tilts, ndf=10 and "
+                         "a 16-voxel-thick volume, for ncu captures (not a bench line)")
     args = ap.parse_args()
     global WORKLOAD_NAME
     if args.case == "large":
@@ -567,6 +569,13 @@ def main():
                   blobs=20000, seed=4)
         WORKLOAD_NAME = ("large 3D CTF ndf=20: 61 tilts +-60 deg, 4096x4096 projections at "
                          "0.8 A/px, 300 kV, Cs 2.7 mm, df 40000 A, volume 4096x4096x512")
+        args.no_cpu = True
+        args.no_serve = True
+    if args.case == "large_profile":
+        WL.update(T=2, H=4096, W=4096, Z=16, D=10, pixel_size=0.8, defocus=40000.0,
+                  blobs=200, seed=4)
+        WORKLOAD_NAME = ("profiling case: 2 tilts, 4096x4096 projections at 0.8 A/px, ndf=10, "
+                         "df 40000 A, volume 4096x4096x16")
         args.no_cpu = True
         args.no_serve = True
     if args.case == "profile":

@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(256 * C, 4 / C) k_column_b4096(const float2 *_
 #pragma unroll
     for (int m = 0; m < 16; ++m) v[m] = make_float2(0.f, 0.f);
   }
-  float2 *buf = smem_cb + c * kB4096Slots;
+  float2 *buf = smem_cb + c * kB4096Stride;
   bfft4096<FLIP, true>(v, buf, buf, roots, l, BlockSync());
   float2 *out = FLIP ? dst + ((size_t)tl * D + d) * kN * half : dst + (size_t)t * kN * half;
   if (kx < half) {
@@ -241,7 +241,7 @@ static cudaError_t column_b4096(const float2 *src, float2 *dst, const int8_t *si
   FftPlan p;
   if (!make_fft_plan(kN, &p)) return cudaErrorInvalidValue;
   constexpr int C = kColC;
-  const size_t smem = (size_t)C * kB4096Slots * sizeof(float2);
+  const size_t smem = (size_t)C * kB4096Stride * sizeof(float2);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_column_b4096<FLIP, C>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -12,19 +12,50 @@
 // 3. exchange: thread l = k0 + 16 k1 gathers n0 = 0..15 from slots
 //    B[k0 + 16 k1 + 257 n0]; 16-point DFT (n0 -> k2): X[l + 256 k2] in v[k2].
 // Two shared-memory exchanges per transform (a Stockham radix-16 transform in
-// shared memory moves the data three times, plus the load and store).  Every
-// exchange hits each 8-byte bank pair exactly twice per warp -- the minimum
-// for 32 eight-byte accesses -- also when the threads of C = 2 or 4 transforms
-// are interleaved (thread = c + C l) and transform c's slots start at
-// c * kB4096Slots (kB4096Slots = 8 mod 16).
+// shared memory moves the data three times, plus the load and store).
+// Eight-byte shared accesses are served a half warp at a time; in every
+// exchange the 16 lanes of a half warp hit 16 distinct 8-byte bank pairs, also
+// when the threads of C = 2 or 4 transforms are interleaved (thread = c + C l)
+// and transform c's slots start at c * kB4096Stride (= 4 mod 16).
 // Conventions: forward exp(-2 pi i/N), inverse exp(+2 pi i/N), unnormalised.
 #pragma once
 
 #include "gnc_fft_pow2.cuh"
+#include "gnc_fft_warp.cuh"
 
 namespace gnc {
 
-constexpr int kB4096Slots = 4216;  // slots of one transform's exchanges
+constexpr int kB4096Slots = 4216;   // slots of one transform's exchanges
+constexpr int kB4096Stride = 4228;  // slot stride of interleaved transforms (4 mod 16)
+
+// 16-point DFT in registers, natural order, with the radix-4 butterflies on
+// packed f32x2 pairs: the operations of dft16 (gnc_fft_pow2.cuh) in the same
+// order, so the results are the same.
+template <bool INV>
+__device__ __forceinline__ void dft16_pk(float2 *x) {
+  pk::c64 a[16];
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) {
+    pk::c64 v0 = pk::pack(x[n2]), v1 = pk::pack(x[4 + n2]), v2 = pk::pack(x[8 + n2]),
+            v3 = pk::pack(x[12 + n2]);
+    pk::dft4<INV>(v0, v1, v2, v3);
+    a[n2 * 4 + 0] = v0;
+    a[n2 * 4 + 1] = v1;
+    a[n2 * 4 + 2] = v2;
+    a[n2 * 4 + 3] = v3;
+  }
+#pragma unroll
+  for (int n2 = 1; n2 < 4; ++n2)
+#pragma unroll
+    for (int k1 = 1; k1 < 4; ++k1)
+      a[n2 * 4 + k1] = pk::pack(w16<INV>(pk::unpack(a[n2 * 4 + k1]), n2 * k1));
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    pk::dft4<INV>(a[k1], a[4 + k1], a[8 + k1], a[12 + k1]);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) x[k1 + 4 * k2] = pk::unpack(a[k1 + 4 * k2]);
+  }
+}
 
 // v[r] *= w^(r base) for r = 1..15, w = exp(-2 pi i / 4096) (conjugate for the
 // inverse): powers 1, 2, 3, 4, 8 and 12 from the table, the others as products
@@ -59,7 +90,7 @@ __device__ __forceinline__ void twiddle16(float2 *v, const float2 *__restrict__ 
 template <bool INV, bool SAME, typename Sync>
 __device__ __forceinline__ void bfft4096(float2 *v, float2 *A, float2 *B,
                                          const float2 *__restrict__ roots, int l, Sync sync) {
-  dft16<INV>(v);
+  dft16_pk<INV>(v);
   twiddle16<INV>(v, roots, l);
 #pragma unroll
   for (int k0 = 0; k0 < 16; ++k0) A[l + 264 * k0] = v[k0];
@@ -69,7 +100,7 @@ __device__ __forceinline__ void bfft4096(float2 *v, float2 *A, float2 *B,
     const float2 *a = A + n0 + 264 * k0;
 #pragma unroll
     for (int n1 = 0; n1 < 16; ++n1) v[n1] = a[16 * n1];
-    dft16<INV>(v);
+    dft16_pk<INV>(v);
     twiddle16<INV>(v, roots, 16 * n0);
     if (SAME) sync();
     float2 *b = B + k0 + 257 * n0;
@@ -79,7 +110,7 @@ __device__ __forceinline__ void bfft4096(float2 *v, float2 *A, float2 *B,
   sync();
 #pragma unroll
   for (int n0 = 0; n0 < 16; ++n0) v[n0] = B[l + 257 * n0];
-  dft16<INV>(v);
+  dft16_pk<INV>(v);
 }
 
 }  // namespace gnc
