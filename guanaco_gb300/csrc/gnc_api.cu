@@ -347,7 +347,7 @@ size_t plan_bytes(const gnc_fbp_desc *d) {
     const size_t per_tilt = D * H * half * sizeof(float2);
     const size_t chunk = std::max<size_t>(1, std::min<size_t>(T, (48ull << 20) / per_tilt));
     b += T * H * half * sizeof(float2) + 2 * chunk * D * H * half * sizeof(float2) +
-         D * H * (half + 1);
+         sign_table_bytes((int)D, (int)H, (int)W);
   }
   b += (Y2 * D * T * W + 8) * kStagedPixelBytes;
   if (d->staging == GNC_STAGE_F16) b += Y2 * D * T * 2;
@@ -453,7 +453,7 @@ int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
       e = cudaEventCreateWithFlags(&p->ev_flip[b], cudaEventDisableTiming);
       if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_rows[b], cudaEventDisableTiming);
     }
-    if (e == cudaSuccess) e = dalloc(p, &p->sign, (size_t)p->D * p->H * (half + 1));
+    if (e == cudaSuccess) e = dalloc(p, &p->sign, sign_table_bytes(p->D, p->H, p->W));
   }
   // +8 pixels: a 16-byte aligned bulk copy of the last row may run past its end
   const size_t elems = (size_t)p->Y2 * p->D * p->T * p->W + 8;
@@ -536,6 +536,7 @@ int gnc_fbp_stage(gnc_fbp_plan *p, const float *d_input, void *stream) {
   r.row_exp = p->row_exp;
   if (p->correct) {
     GNC_CUDA(launch_sign_table(p->sargs, p->sign, s));
+    GNC_CUDA(launch_sign_pack(p->sign, p->D, p->H, p->W, s));
     GNC_CUDA(launch_rfft_rows(d_input, p->spec, p->T, p->H, p->W, s));
     GNC_CUDA(launch_column_fft(p->spec, p->T, p->H, p->W, s));
     r.input_spectra = 1;
@@ -648,6 +649,7 @@ static int execute_host_pipelined(gnc_fbp_plan *p, const float *h_input, float *
   r.row_exp = p->row_exp;
   if (p->correct) {
     GNC_CUDA(launch_sign_table(p->sargs, p->sign, s));
+    GNC_CUDA(launch_sign_pack(p->sign, p->D, p->H, p->W, s));
     r.input_spectra = 1;
   } else {
     r.input_spectra = 0;
@@ -742,6 +744,7 @@ int gnc_fbp_correct(gnc_fbp_plan *p, const float *d_proj, float *d_corrected, vo
   GNC_REQUIRE(p != nullptr && p->correct && d_proj != nullptr && d_corrected != nullptr);
   cudaStream_t s = (cudaStream_t)stream;
   GNC_CUDA(launch_sign_table(p->sargs, p->sign, s));
+  GNC_CUDA(launch_sign_pack(p->sign, p->D, p->H, p->W, s));
   GNC_CUDA(launch_rfft_rows(d_proj, p->spec, p->T, p->H, p->W, s));
   GNC_CUDA(launch_column_fft(p->spec, p->T, p->H, p->W, s));
   RowStageArgs r{};
@@ -766,7 +769,8 @@ int gnc_fbp_launches(const gnc_fbp_plan *p) {
   if (!p) return 0;
   if (!p->correct) return 2;  // row stage, backprojection
   const int chunks = (p->T + p->chunk - 1) / p->chunk;
-  return 3 + 2 * chunks + 1;  // sign table, row and column transforms, per chunk flip + rows, BP
+  // sign table (+ its packed copy), row and column transforms, per chunk flip + rows, BP
+  return 3 + (sign_pack_used(p->H) ? 1 : 0) + 2 * chunks + 1;
 }
 
 int gnc_fbp_check(gnc_fbp_plan *p, void *stream) {
@@ -984,7 +988,7 @@ int gnc_correct(const float *image, const float *ctf, float *rec, size_t xsize, 
   if (e == cudaSuccess) e = cudaMallocAsync((void **)&dctf, D * img * sizeof(float2), s);
   if (e == cudaSuccess) e = cudaMallocAsync((void **)&spec, H * half * sizeof(float2), s);
   if (e == cudaSuccess) e = cudaMallocAsync((void **)&g, D * H * half * sizeof(float2), s);
-  if (e == cudaSuccess) e = cudaMallocAsync((void **)&sign, D * H * (half + 1), s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void **)&sign, sign_table_bytes(D, H, W), s);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(dimg, image, img * sizeof(float), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess)
@@ -994,6 +998,7 @@ int gnc_correct(const float *image, const float *ctf, float *rec, size_t xsize, 
         dctf, D, H, W, sign);
     e = cudaGetLastError();
   }
+  if (e == cudaSuccess) e = launch_sign_pack(sign, D, H, W, s);
   if (e == cudaSuccess) e = launch_rfft_rows(dimg, spec, 1, H, W, s);
   if (e == cudaSuccess) e = launch_column_fft(spec, 1, H, W, s);
   if (e == cudaSuccess) e = launch_column_flip(spec, g, sign, 0, 1, D, H, W, s);

@@ -41,7 +41,7 @@ constexpr int kColC = 4;
 template <bool FLIP, int C>
 __global__ void __launch_bounds__(256 * C, 4 / C) k_column_b4096(const float2 *__restrict__ src,
                                                              float2 *__restrict__ dst,
-                                                             const int8_t *__restrict__ sign,
+                                                             const unsigned long long *__restrict__ sign,
                                                              int t0, int D, int W,
                                                              const float2 *__restrict__ roots) {
   extern __shared__ float2 smem_cb[];
@@ -53,24 +53,27 @@ __global__ void __launch_bounds__(256 * C, 4 / C) k_column_b4096(const float2 *_
   const int t = t0 + tl;
   const float2 *F = src + (size_t)t * kN * half;
   const int sw = half + 1;
-  const int8_t *sg = FLIP ? sign + (size_t)d * kN * sw : nullptr;
+  // the 16 signs of rows l + 256 m: one packed entry (d, l, kx)
+  const unsigned long long *sg = FLIP ? sign + ((size_t)d * 256 + l) * sw : nullptr;
   float2 v[16];
   if (kx < half) {
 #pragma unroll
     for (int m = 0; m < 16; ++m) v[m] = F[(size_t)(l + 256 * m) * half + kx];
     if (FLIP && kx == 0) {
+      const unsigned long long wd = sg[0], wn = sg[half];
 #pragma unroll
       for (int m = 0; m < 16; ++m) {
         const int ky = l + 256 * m;
         const float2 mr = F[(size_t)((kN - ky) & (kN - 1)) * half];
-        const float sdc = 0.5f * (float)sg[(size_t)ky * sw];
-        const float sny = 0.5f * (float)sg[(size_t)ky * sw + half];
+        const float sdc = 0.5f * (float)packed_sign(wd, m);
+        const float sny = 0.5f * (float)packed_sign(wn, m);
         const float a = 0.5f * (sdc + sny), b = 0.5f * (sdc - sny);
         v[m] = make_float2(a * v[m].x + b * mr.x, a * v[m].y - b * mr.y);
       }
     } else if (FLIP) {
+      const unsigned long long w = sg[kx];
 #pragma unroll
-      for (int m = 0; m < 16; ++m) v[m] = scale2(0.5f * (float)sg[(size_t)(l + 256 * m) * sw + kx], v[m]);
+      for (int m = 0; m < 16; ++m) v[m] = scale2(0.5f * (float)packed_sign(w, m), v[m]);
     }
   } else {
 #pragma unroll
@@ -250,7 +253,9 @@ static cudaError_t column_b4096(const float2 *src, float2 *dst, const int8_t *si
   }
   const int half = W / 2;
   dim3 grid((half + C - 1) / C, FLIP ? D : 1, nt);
-  k_column_b4096<FLIP, C><<<grid, 256 * C, smem, s>>>(src, dst, sign, t0, D, W, p.roots);
+  const unsigned long long *packed = FLIP ? sign_packed(sign, D, kN, W) : nullptr;
+  if (((uintptr_t)packed & 7) != 0) return cudaErrorMisalignedAddress;  // 8-byte loads
+  k_column_b4096<FLIP, C><<<grid, 256 * C, smem, s>>>(src, dst, packed, t0, D, W, p.roots);
   return cudaGetLastError();
 }
 

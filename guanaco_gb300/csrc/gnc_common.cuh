@@ -66,6 +66,17 @@ cudaError_t launch_column_fft(float2 *spec, int T, int H, int W, cudaStream_t s)
 // [t0, t0 + nt) of the column-transformed spectra: spec (T, H, W/2) ->
 // g (nt, D, H, W/2).
 // sign: (D, H, W/2 + 1) int8 holding 2 * (s(k) + s(-k)) / 2.
+// Bytes of a sign table allocation for (D, H, W): the int8 table (D, H, W/2+1)
+// and, for 1024 and 4096 rows, the packed copy the column kernels of those
+// sizes read (written by launch_sign_pack after launch_sign_table).
+size_t sign_table_bytes(int D, int H, int W);
+bool sign_pack_used(int H);
+const unsigned long long *sign_packed(const int8_t *sign, int D, int H, int W);
+cudaError_t launch_sign_pack(int8_t *sign, int D, int H, int W, cudaStream_t s);
+// Sign m (0..15) of a packed word.
+__device__ __forceinline__ int packed_sign(unsigned long long w, int m) {
+  return (int)((w >> (3 * m)) & 7ull) - 2;
+}
 cudaError_t launch_column_flip(const float2 *spec, float2 *g, const int8_t *sign, int t0, int nt,
                                int D, int H, int W, cudaStream_t s);
 

@@ -4,6 +4,8 @@
 // (include/guanaco/ctf.h), without fused multiply-adds.
 #include <math.h>
 
+#include <algorithm>
+
 #include "gnc_common.cuh"
 
 namespace gnc {
@@ -109,6 +111,80 @@ void fill_sign_screen(SignTableArgs *a) {
   a->f_s2p = (float)sin(2 * a->Pa);
   a->f_ips2 = (float)(a->inv_ps * a->inv_ps);
   a->f_lca = (float)(a->l * a->Ca * a->inv_ps * a->inv_ps);
+}
+
+// Packed signs for the column kernels of 1024 and 4096 rows, whose threads
+// each phase-flip rows r + R m (m < M) of one column: those M signs sit
+// together, 3 bits each (s + 2 for s in -2..2), 16 to a 64-bit word, entry
+// (d, r, kx) = M / 16 words at ((d R + r) (W/2 + 1) + kx) M / 16.  The packed
+// table follows the int8 table in the same allocation, 256-byte aligned.
+static bool sign_pack_shape(int H, int *R, int *M) {
+  if (H == 1024) {
+    *R = 32;
+    *M = 32;
+    return true;
+  }
+  if (H == 4096) {
+    *R = 256;
+    *M = 16;
+    return true;
+  }
+  return false;
+}
+
+bool sign_pack_used(int H) {
+  int R, M;
+  return sign_pack_shape(H, &R, &M);
+}
+
+static size_t sign_int8_bytes(int D, int H, int W) {
+  return ((size_t)D * H * (W / 2 + 1) + 255) / 256 * 256;
+}
+
+size_t sign_table_bytes(int D, int H, int W) {
+  int R, M;
+  if (!sign_pack_shape(H, &R, &M)) return (size_t)D * H * (W / 2 + 1);
+  return sign_int8_bytes(D, H, W) + (size_t)D * R * (W / 2 + 1) * (M / 16) * 8;
+}
+
+const unsigned long long *sign_packed(const int8_t *sign, int D, int H, int W) {
+  return (const unsigned long long *)(sign + sign_int8_bytes(D, H, W));
+}
+
+template <int R, int M>
+__global__ void k_sign_pack(const int8_t *__restrict__ sign, int D, int W,
+                            unsigned long long *__restrict__ out) {
+  constexpr int H = R * M, NW = M / 16;
+  const int sw = W / 2 + 1;
+  const long n = (long)D * R * sw;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long)gridDim.x * blockDim.x) {
+    const int kx = (int)(i % sw);
+    const long dr = i / sw;
+    const int r = (int)(dr % R), d = (int)(dr / R);
+    const int8_t *src = sign + ((size_t)d * H + r) * sw + kx;
+    unsigned long long w[NW];
+#pragma unroll
+    for (int j = 0; j < NW; ++j) w[j] = 0ull;
+#pragma unroll
+    for (int m = 0; m < M; ++m)
+      w[m >> 4] |= (unsigned long long)((src[(size_t)R * m * sw] + 2) & 7) << (3 * (m & 15));
+#pragma unroll
+    for (int j = 0; j < NW; ++j) out[i * NW + j] = w[j];
+  }
+}
+
+cudaError_t launch_sign_pack(int8_t *sign, int D, int H, int W, cudaStream_t s) {
+  int R, M;
+  if (!sign_pack_shape(H, &R, &M)) return cudaSuccess;
+  unsigned long long *out = (unsigned long long *)(sign + sign_int8_bytes(D, H, W));
+  const long n = (long)D * R * (W / 2 + 1);
+  const int blocks = (int)std::min<long>((n + 255) / 256, 152 * 8);
+  if (H == 1024)
+    k_sign_pack<32, 32><<<blocks, 256, 0, s>>>(sign, D, W, out);
+  else
+    k_sign_pack<256, 16><<<blocks, 256, 0, s>>>(sign, D, W, out);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_sign_table(const SignTableArgs &a, int8_t *out, cudaStream_t s) {

@@ -76,8 +76,8 @@ __global__ void __launch_bounds__(256) k_rfft_rows_w1024(const float *__restrict
 template <bool FLIP>
 __global__ void __launch_bounds__(256, 2) k_column_w1024(const float2 *__restrict__ src,
                                                       float2 *__restrict__ dst,
-                                                      const int8_t *__restrict__ sign, int t0,
-                                                      int D, int W,
+                                                      const ulonglong2 *__restrict__ sign,
+                                                      int t0, int D, int W,
                                                       const float2 *__restrict__ roots) {
   constexpr int C = 8, P = 9;
   extern __shared__ float2 smem_w[];
@@ -92,29 +92,32 @@ __global__ void __launch_bounds__(256, 2) k_column_w1024(const float2 *__restric
   const int t = t0 + tl;
   const float2 *F = src + (size_t)t * kN * half;
   const int sw = half + 1;
-  const int8_t *sg = FLIP ? sign + (size_t)d * kN * sw : nullptr;
-  // each thread moves one column (c) of rows r0 + 32 j: all 32 loads in flight
+  // each thread moves one column (c) of rows r0 + 32 j: all 32 loads in flight;
+  // their 32 signs are one packed entry (d, r0, kx)
   const int c = threadIdx.x & (C - 1), r0 = threadIdx.x / C;
   const int kx = c0 + c;
+  const ulonglong2 *sg = FLIP ? sign + ((size_t)d * 32 + r0) * sw : nullptr;
   {
     float2 r[32];
     if (kx < half) {
 #pragma unroll
       for (int j = 0; j < 32; ++j) r[j] = F[(size_t)(r0 + 32 * j) * half + kx];
       if (FLIP && kx == 0) {
+        const ulonglong2 wd = sg[0], wn = sg[half];
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
           const int ky = r0 + 32 * j;
           const float2 m = F[(size_t)((kN - ky) & (kN - 1)) * half];
-          const float sdc = 0.5f * (float)sg[(size_t)ky * sw];
-          const float sny = 0.5f * (float)sg[(size_t)ky * sw + half];
+          const float sdc = 0.5f * (float)packed_sign(j < 16 ? wd.x : wd.y, j & 15);
+          const float sny = 0.5f * (float)packed_sign(j < 16 ? wn.x : wn.y, j & 15);
           const float a = 0.5f * (sdc + sny), b = 0.5f * (sdc - sny);
           r[j] = make_float2(a * r[j].x + b * m.x, a * r[j].y - b * m.y);
         }
       } else if (FLIP) {
+        const ulonglong2 w = sg[kx];
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
-          const float f = 0.5f * (float)sg[(size_t)(r0 + 32 * j) * sw + kx];
+          const float f = 0.5f * (float)packed_sign(j < 16 ? w.x : w.y, j & 15);
           r[j] = make_float2(f * r[j].x, f * r[j].y);
         }
       }
@@ -370,8 +373,10 @@ static cudaError_t column_w1024(const float2 *src, float2 *dst, const int8_t *si
     attr = true;
   }
   const int half = W / 2;
+  const ulonglong2 *packed = FLIP ? (const ulonglong2 *)sign_packed(sign, D, kN, W) : nullptr;
+  if (((uintptr_t)packed & 15) != 0) return cudaErrorMisalignedAddress;  // 16-byte loads
   dim3 grid((half + 7) / 8, FLIP ? D : 1, nt);
-  k_column_w1024<FLIP><<<grid, 256, smem, s>>>(src, dst, sign, t0, D, W, roots);
+  k_column_w1024<FLIP><<<grid, 256, smem, s>>>(src, dst, packed, t0, D, W, roots);
   return cudaGetLastError();
 }
 
