@@ -28,8 +28,8 @@
 // (both rows' values and differences to the next pixel), the interpolation
 // one half2 FMA and the sum one f32x2 FMA with (scale 2^-e_a, scale 2^-e_b)
 // for that row pair and slab.  The FP16 form reads half the shared-memory
-// bytes per voxel-tilt; it holds 4 voxels x 16 rows per thread (FP32: 8 x 8)
-// so that the per-voxel work is shared by more rows.
+// bytes per voxel-tilt.  Both forms hold 8 voxels (4 in x, 2 in z) x 8 rows
+// per thread on a 64 x 32 (x, z) tile.
 #include <cmath>
 #include <type_traits>
 
@@ -142,7 +142,7 @@ struct TiltParams {
 
 template <int RP, int KMAX, int G, bool F16>
 struct FastBp {
-  static constexpr int A = 2, B = F16 ? 2 : 4;    // voxels per thread in x and z
+  static constexpr int A = 4, B = 2;              // voxels per thread in x and z
   static constexpr int TCH = RP * KMAX > 16 ? 64 : 128;  // tilts whose parameters are held
   static constexpr int WX = 4, WZ = 2;            // warps per block in x and z
   static constexpr int TX = 4 * A * WX;           // tile width (x)
@@ -517,8 +517,8 @@ cudaError_t launch_backproject_fast(const BpArgs &a, cudaStream_t s) {
   // <row pairs per thread, slabs per tile, tilts per group>: two buffers of
   // G * RP * KMAX slots within two blocks per SM
   if (need <= 2)
-    return f16 ? launch_fast<8, 2, 6, true>(a, s) : launch_fast<4, 2, 8, false>(a, s);
-  return f16 ? launch_fast<8, 4, 3, true>(a, s) : launch_fast<4, 4, 4, false>(a, s);
+    return f16 ? launch_fast<4, 2, 8, true>(a, s) : launch_fast<4, 2, 8, false>(a, s);
+  return f16 ? launch_fast<4, 4, 4, true>(a, s) : launch_fast<4, 4, 4, false>(a, s);
 }
 
 }  // namespace gnc
