@@ -46,7 +46,7 @@ WORKLOAD_NAME = ("3D CTF ndf=10: 61 tilts +-60 deg, 1024x1024 projections at 1.0
                  "300 kV, Cs 2.7 mm, df 30000 A, volume 1024x1024x300")
 # DRAM traffic of one k_bp_fast launch on this workload, from the ncu capture
 # summarised in profiles/k_bp_fast_3dctf_ndf10.md (bytes read + written).
-BP_TRAFFIC_BYTES = {"f32": 2.31e9, "f16": 1.767e9}
+BP_TRAFFIC_BYTES = {"f32": 2.330e9, "f16": 2.332e9}
 
 
 def angles_rad():
