@@ -11,6 +11,8 @@
   (``guanaco_gb300.mrc`` reads and writes MRC2014 with FEI1 headers).
 * ``serve.Server`` -- the request server: many tilt series of mixed shapes at
   once, with continuous batching on one GPU.
+* ``plot.generate_ctf`` -- the CTF images of a defocus series, computed on the
+  GPU and written as a complex64 MRC stack.
 """
 from . import detail  # noqa: F401
 from .api import (  # noqa: F401
@@ -27,5 +29,6 @@ from .api import (  # noqa: F401
     reconstruct_file,
 )
 from .fbp import FbpDesc, FbpPlan  # noqa: F401
+from . import plot  # noqa: F401
 
 __version__ = "0.1.0"

@@ -125,6 +125,8 @@ SIGNATURES = {
     "gnc_ctf_eval": (c_int, [ctypes.POINTER(GncCtf), c_int, c_void, c_void, c_size, c_void]),
     "gnc_ctf_grid": (c_int, [ctypes.POINTER(GncCtf), c_int, c_size, c_size, c_double, c_void]),
     "gnc_q_and_theta": (c_int, [c_size, c_size, c_double, c_void, c_void]),
+    "gnc_ctf_image_device": (c_int, [ctypes.POINTER(GncCtf), c_int, c_void, c_int, c_size,
+                                     c_size, c_double, c_void, c_void]),
     "gnc_fbp_plan_create": (c_int, [ctypes.POINTER(GncFbpDesc), ctypes.POINTER(c_void)]),
     "gnc_fbp_plan_destroy": (c_int, [c_void]),
     "gnc_fbp_workspace_bytes": (c_size, [c_void]),

@@ -6,6 +6,7 @@
 
 #include <algorithm>
 
+#include "../../include/guanaco_gb300.h"
 #include "gnc_common.cuh"
 
 namespace gnc {
@@ -200,7 +201,6 @@ cudaError_t launch_sign_table(const SignTableArgs &a, int8_t *out, cudaStream_t 
 // ---------------------------------------------------------------------------
 // Host CTF functions (include/guanaco/ctf.h), exported through the C ABI.
 // ---------------------------------------------------------------------------
-#include "../../include/guanaco_gb300.h"
 
 namespace {
 const double kC = 2.99792458e8;        // constants.h:31
@@ -208,22 +208,103 @@ const double kE = 1.602176634e-19;     // constants.h:32
 const double kMe = 9.1093837015e-31;   // constants.h:33
 const double kH = 6.62607004e-34;      // constants.h:34
 const double kMtoA = 1e10;             // constants.h:35
+}  // namespace
 
-double log_Es(const gnc_ctf *c, double q, double theta) {  // ctf.h:188-195
-  double df = c->df + c->Ca * cos(2 * (theta - c->Pa));
-  double u = 1 + 2 * M_PI * M_PI * c->theta_c * c->theta_c * c->dd * c->dd * q * q;
-  double v = c->Cs * c->l * c->l * c->l * q * q * q - df * c->l * q;
-  return -(M_PI * M_PI * c->theta_c * c->theta_c * v * v / (c->l * c->l * u));
+namespace gnc {
+
+__host__ __device__ inline double log_Es(const gnc_ctf &c, double q, double theta) {  // ctf.h:188-195
+  double df = c.df + c.Ca * cos(2 * (theta - c.Pa));
+  double u = 1 + 2 * M_PI * M_PI * c.theta_c * c.theta_c * c.dd * c.dd * q * q;
+  double v = c.Cs * c.l * c.l * c.l * q * q * q - df * c.l * q;
+  return -(M_PI * M_PI * c.theta_c * c.theta_c * v * v / (c.l * c.l * u));
 }
-double log_Et(const gnc_ctf *c, double q) {  // ctf.h:204-209
-  double u = 1 + 2 * M_PI * M_PI * c->theta_c * c->theta_c * c->dd * c->dd * q * q;
-  return -(M_PI * M_PI * c->l * c->l * c->dd * c->dd * q * q * q * q / (2 * u));
+__host__ __device__ inline double log_Et(const gnc_ctf &c, double q) {  // ctf.h:204-209
+  double u = 1 + 2 * M_PI * M_PI * c.theta_c * c.theta_c * c.dd * c.dd * q * q;
+  return -(M_PI * M_PI * c.l * c.l * c.dd * c.dd * q * q * q * q / (2 * u));
 }
-double env_A(const gnc_ctf *c, double q) {  // ctf.h:218-223
-  double u = 1 + 2 * M_PI * M_PI * c->theta_c * c->theta_c * c->dd * c->dd * q * q;
+__host__ __device__ inline double env_A(const gnc_ctf &c, double q) {  // ctf.h:218-223
+  double u = 1 + 2 * M_PI * M_PI * c.theta_c * c.theta_c * c.dd * c.dd * q * q;
   return 1 / sqrt(u);
 }
-}  // namespace
+
+// One CTF quantity at (q, theta); complex kinds fill re and im, the others re.
+// False for an unknown kind.  The same code runs on the host (gnc_ctf_eval)
+// and in k_ctf_image.
+__host__ __device__ inline bool ctf_value(const gnc_ctf &c, int kind, double q, double t,
+                                          double *re, double *im) {
+  switch (kind) {
+    case GNC_CTF_FULL: {  // ctf.h:250-257
+      double x = chi(c.l, c.df, c.Cs, c.Ca, c.Pa, q, t);
+      double mag = env_A(c, q) * exp(log_Es(c, q, t) + log_Et(c, q));
+      *re = mag * cos(-(x - c.phi));
+      *im = mag * sin(-(x - c.phi));
+      return true;
+    }
+    case GNC_CTF_SIMPLE: {  // ctf.h:269-273
+      double x = chi(c.l, c.df, c.Cs, c.Ca, c.Pa, q, t);
+      *re = cos(-(x - c.phi));
+      *im = sin(-(x - c.phi));
+      return true;
+    }
+    case GNC_CTF_SIMPLE_REAL:  // ctf.h:285-288
+      *re = cos(-(chi(c.l, c.df, c.Cs, c.Ca, c.Pa, q, t) - c.phi));
+      return true;
+    case GNC_CTF_SIMPLE_IMAG:  // ctf.h:300-303
+      *re = sin(-(chi(c.l, c.df, c.Cs, c.Ca, c.Pa, q, t) - c.phi));
+      return true;
+    case GNC_CTF_CHI:
+      *re = chi(c.l, c.df, c.Cs, c.Ca, c.Pa, q, t);
+      return true;
+    case GNC_CTF_ES:  // ctf.h:314-319
+      *re = exp(log_Es(c, q, t));
+      return true;
+    case GNC_CTF_ET:  // ctf.h:329-332
+      *re = exp(log_Et(c, q));
+      return true;
+  }
+  return false;
+}
+
+__host__ __device__ inline bool ctf_kind_complex(int kind) {
+  return kind == GNC_CTF_FULL || kind == GNC_CTF_SIMPLE;
+}
+
+// CTF images of up to kCtfImageSlabs defoci per launch: slab d of the launch is
+// the (h, w) FFT-ordered grid (ctf.h:466-557) at defocus df[d], written as
+// float32 (complex64 for the complex kinds), (nd, h, w).
+constexpr int kCtfImageSlabs = 64;
+struct CtfImageArgs {
+  gnc_ctf c;
+  int kind, nd;
+  long w, h;
+  double inv_ps;
+  double df[kCtfImageSlabs];
+};
+
+__global__ void k_ctf_image(CtfImageArgs a, float *__restrict__ out) {
+  const long plane = a.w * a.h, n = plane * a.nd;
+  const bool cplx = ctf_kind_complex(a.kind);
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long)gridDim.x * blockDim.x) {
+    const int d = (int)(i / plane);
+    const long p = i - (long)d * plane;
+    const long y = p / a.w, x = p - y * a.w;
+    double q, theta;
+    r_and_theta(x, y, a.w, a.h, a.inv_ps, true, &q, &theta);
+    gnc_ctf c = a.c;
+    c.df = a.df[d];
+    double re = 0.0, im = 0.0;
+    ctf_value(c, a.kind, q, theta, &re, &im);
+    if (cplx) {
+      out[2 * i] = (float)re;
+      out[2 * i + 1] = (float)im;
+    } else {
+      out[i] = (float)re;
+    }
+  }
+}
+
+}  // namespace gnc
 
 extern "C" {
 
@@ -251,41 +332,16 @@ int gnc_ctf_eval(const gnc_ctf *c, int kind, const double *q, const double *thet
     gnc::set_error("gnc_ctf_eval: null pointer");
     return GNC_ERR_INVALID_ARGUMENT;
   }
+  if (kind < GNC_CTF_FULL || kind > GNC_CTF_ET) {
+    gnc::set_error("gnc_ctf_eval: unknown kind");
+    return GNC_ERR_INVALID_ARGUMENT;
+  }
+  const int cplx = gnc::ctf_kind_complex(kind) ? 2 : 1;
   for (size_t i = 0; i < n; ++i) {
-    double qi = q[i], ti = theta ? theta[i] : 0.0;
-    switch (kind) {
-      case GNC_CTF_FULL: {  // ctf.h:250-257
-        double x = gnc::chi(c->l, c->df, c->Cs, c->Ca, c->Pa, qi, ti);
-        double mag = env_A(c, qi) * exp(log_Es(c, qi, ti) + log_Et(c, qi));
-        out[2 * i] = mag * cos(-(x - c->phi));
-        out[2 * i + 1] = mag * sin(-(x - c->phi));
-        break;
-      }
-      case GNC_CTF_SIMPLE: {  // ctf.h:269-273
-        double x = gnc::chi(c->l, c->df, c->Cs, c->Ca, c->Pa, qi, ti);
-        out[2 * i] = cos(-(x - c->phi));
-        out[2 * i + 1] = sin(-(x - c->phi));
-        break;
-      }
-      case GNC_CTF_SIMPLE_REAL:  // ctf.h:285-288
-        out[i] = cos(-(gnc::chi(c->l, c->df, c->Cs, c->Ca, c->Pa, qi, ti) - c->phi));
-        break;
-      case GNC_CTF_SIMPLE_IMAG:  // ctf.h:300-303
-        out[i] = sin(-(gnc::chi(c->l, c->df, c->Cs, c->Ca, c->Pa, qi, ti) - c->phi));
-        break;
-      case GNC_CTF_CHI:
-        out[i] = gnc::chi(c->l, c->df, c->Cs, c->Ca, c->Pa, qi, ti);
-        break;
-      case GNC_CTF_ES:  // ctf.h:314-319
-        out[i] = exp(log_Es(c, qi, ti));
-        break;
-      case GNC_CTF_ET:  // ctf.h:329-332
-        out[i] = exp(log_Et(c, qi));
-        break;
-      default:
-        gnc::set_error("gnc_ctf_eval: unknown kind");
-        return GNC_ERR_INVALID_ARGUMENT;
-    }
+    double re = 0.0, im = 0.0;
+    gnc::ctf_value(*c, kind, q[i], theta ? theta[i] : 0.0, &re, &im);
+    out[cplx * i] = re;
+    if (cplx == 2) out[2 * i + 1] = im;
   }
   return GNC_OK;
 }
@@ -300,6 +356,37 @@ int gnc_q_and_theta(size_t w, size_t h, double ps, double *q, double *theta) {
     for (size_t i = 0; i < w; ++i)
       gnc::r_and_theta((long)i, (long)j, (long)w, (long)h, inv_ps, true, &q[j * w + i],
                        &theta[j * w + i]);
+  return GNC_OK;
+}
+
+int gnc_ctf_image_device(const gnc_ctf *c, int kind, const double *defocus, int num_defocus,
+                         size_t w, size_t h, double ps, void *d_out, void *stream) {
+  if (!c || !defocus || !d_out || !(ps > 0) || num_defocus < 1 || w < 1 || h < 1 ||
+      kind < GNC_CTF_FULL || kind > GNC_CTF_ET) {
+    gnc::set_error("gnc_ctf_image_device: null pointer, ps <= 0, no defocus, empty image or "
+                   "unknown kind");
+    return GNC_ERR_INVALID_ARGUMENT;
+  }
+  const size_t plane = w * h * (gnc::ctf_kind_complex(kind) ? 2 : 1);
+  cudaStream_t s = (cudaStream_t)stream;
+  for (int d0 = 0; d0 < num_defocus; d0 += gnc::kCtfImageSlabs) {
+    gnc::CtfImageArgs a{};
+    a.c = *c;
+    a.kind = kind;
+    a.nd = std::min(gnc::kCtfImageSlabs, num_defocus - d0);
+    a.w = (long)w;
+    a.h = (long)h;
+    a.inv_ps = 1.0 / ps;
+    for (int d = 0; d < a.nd; ++d) a.df[d] = defocus[d0 + d];
+    const long n = (long)(w * h) * a.nd;
+    const int blocks = (int)std::min<long>((n + 255) / 256, 152 * 16);
+    gnc::k_ctf_image<<<blocks, 256, 0, s>>>(a, (float *)d_out + (size_t)d0 * plane);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      gnc::set_error(std::string("gnc_ctf_image_device: ") + cudaGetErrorString(e));
+      return GNC_ERR_CUDA;
+    }
+  }
   return GNC_OK;
 }
 

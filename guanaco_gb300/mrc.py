@@ -9,7 +9,8 @@ the MRC2014 format those functions use:
   (mx, my, mz), cell dimensions (voxel size = cell / sampling), space group
   (0 image stack, 1 volume, 401 stack of volumes), extended-header size and
   type, origin, ``MAP `` tag, machine stamp, statistics and labels;
-* data modes 0 (int8), 1 (int16), 2 (float32), 6 (uint16) and 12 (float16),
+* data modes 0 (int8), 1 (int16), 2 (float32), 4 (complex64: CTF images), 6
+  (uint16) and 12 (float16),
   read as arrays of that type, X fastest;
 * the FEI1 extended header: one record per image (per tilt and defocus for a
   corrected stack) whose first int32 is the record size; the reference uses
@@ -39,8 +40,8 @@ MAIN_HEADER = np.dtype([
 ])
 assert MAIN_HEADER.itemsize == 1024
 
-MODES = {0: np.dtype("i1"), 1: np.dtype("<i2"), 2: np.dtype("<f4"), 6: np.dtype("<u2"),
-         12: np.dtype("<f2")}
+MODES = {0: np.dtype("i1"), 1: np.dtype("<i2"), 2: np.dtype("<f4"), 4: np.dtype("<c8"),
+         6: np.dtype("<u2"), 12: np.dtype("<f2")}
 MODE_OF = {v: k for k, v in MODES.items()}
 
 # FEI1 extended-header record: the fields the reference uses, at their byte
@@ -77,7 +78,10 @@ class MrcFile:
 
     def close(self):
         if self._writable:
-            d = np.asarray(self.data, dtype=np.float64) if self.data.size < (1 << 26) else None
+            d = None
+            if self.data.size < (1 << 26):  # statistics of the magnitude for complex data
+                d = np.abs(self.data) if np.iscomplexobj(self.data) else self.data
+                d = np.asarray(d, dtype=np.float64)
             h = self.header
             if d is not None and d.size:
                 h["dmin"], h["dmax"], h["dmean"] = d.min(), d.max(), d.mean()

@@ -147,6 +147,16 @@ GNC_API int gnc_ctf_eval(const gnc_ctf *c, int kind, const double *q, const doub
  * (src/guanaco/detail/ext/ctf.h:41-56). */
 GNC_API int gnc_ctf_grid(const gnc_ctf *c, int kind, size_t w, size_t h, double ps, double *out);
 GNC_API int gnc_q_and_theta(size_t w, size_t h, double ps, double *q, double *theta);
+/* CTF image stack computed on the device: slab d is the (h, w) FFT-ordered grid
+ * of `kind` (as gnc_ctf_grid, double arithmetic) with the defocus replaced by
+ * defocus[d] (host array of num_defocus values; c->df is not used), written to
+ * d_out as complex64 (kinds FULL, SIMPLE) or float32 (the others), shape
+ * (num_defocus, h, w), on `stream`.  Replaces the per-slab host loops of
+ * generate_ctf (src/guanaco/plot.py:175-284, CTF.get_ctf per defocus) and
+ * get_ctf_array (src/guanaco/detail/correct.py:157-214). */
+GNC_API int gnc_ctf_image_device(const gnc_ctf *c, int kind, const double *defocus,
+                                 int num_defocus, size_t w, size_t h, double ps, void *d_out,
+                                 void *stream);
 
 /* ------------------------------------------------------------------------
  * Whole-series 3D-CTF FBP.  One plan replaces the reference's

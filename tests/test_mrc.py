@@ -1,6 +1,7 @@
 """MRC2014 files (host only): the main-header and FEI1 record layout at their
-byte offsets, data round trips in every supported mode, image stacks, volumes
-and the 4D corrected stack (stack of volumes)."""
+byte offsets, data round trips in every supported mode (complex64 for CTF
+images included), image stacks, volumes and the 4D corrected stack (stack of
+volumes)."""
 import numpy as np
 import pytest
 
@@ -33,11 +34,14 @@ def test_header_and_fei1_record_offsets(tmp_path):
     np.testing.assert_array_equal(data0, [0, 1, 2, 3])
 
 
-@pytest.mark.parametrize("dtype", [np.float32, np.int16, np.uint16, np.int8, np.float16])
+@pytest.mark.parametrize("dtype", [np.float32, np.int16, np.uint16, np.int8, np.float16,
+                                   np.complex64])
 def test_round_trip_modes(tmp_path, dtype):
     p = str(tmp_path / "v.mrc")
     rng = np.random.default_rng(1)
     a = (rng.standard_normal((4, 5, 7)) * 50).astype(dtype)
+    if np.dtype(dtype).kind == "c":
+        a = a + 1j * (rng.standard_normal(a.shape) * 50).astype(np.float32)
     with mrc.new_mrc(p, a.shape, dtype, voxel_size=(1.0, 2.0, 3.0)) as f:
         f.data[...] = a
     g = mrc.open_mrc(p)
@@ -45,6 +49,8 @@ def test_round_trip_modes(tmp_path, dtype):
     np.testing.assert_array_equal(np.asarray(g.data), a)
     assert g.voxel_size == {"x": 1.0, "y": 2.0, "z": 3.0}
     assert int(g.header["ispg"]) == 1 and g.extended_header is None
+    assert int(g.header["mode"]) == {np.float32: 2, np.int16: 1, np.uint16: 6, np.int8: 0,
+                                     np.float16: 12, np.complex64: 4}[dtype]
 
 
 def test_corrected_stack_of_volumes(tmp_path):
