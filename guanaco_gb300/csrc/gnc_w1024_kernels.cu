@@ -92,21 +92,24 @@ __global__ void __launch_bounds__(256, 2) k_column_w1024(const float2 *__restric
   const int t = t0 + tl;
   const float2 *F = src + (size_t)t * kN * half;
   const int sw = half + 1;
-  // each thread moves one column (c) of rows r0 + 32 j: all 32 loads in flight;
-  // their 32 signs are one packed entry (d, r0, kx)
+  // each thread moves one column (c) of rows y0 + 32 j: all 32 loads in flight;
+  // their 32 signs are one packed entry (d, y0, kx).  y0 permutes the 32
+  // row residues so that the two rows of a half warp are 8 apart: with the
+  // 9-float2 pitch their tile slots then fall in bank pairs 0-7 and 8-15.
   const int c = threadIdx.x & (C - 1), r0 = threadIdx.x / C;
+  const int y0 = (r0 & 16) + ((r0 >> 1) & 7) + 8 * (r0 & 1);
   const int kx = c0 + c;
-  const ulonglong2 *sg = FLIP ? sign + ((size_t)d * 32 + r0) * sw : nullptr;
+  const ulonglong2 *sg = FLIP ? sign + ((size_t)d * 32 + y0) * sw : nullptr;
   {
     float2 r[32];
     if (kx < half) {
 #pragma unroll
-      for (int j = 0; j < 32; ++j) r[j] = F[(size_t)(r0 + 32 * j) * half + kx];
+      for (int j = 0; j < 32; ++j) r[j] = F[(size_t)(y0 + 32 * j) * half + kx];
       if (FLIP && kx == 0) {
         const ulonglong2 wd = sg[0], wn = sg[half];
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
-          const int ky = r0 + 32 * j;
+          const int ky = y0 + 32 * j;
           const float2 m = F[(size_t)((kN - ky) & (kN - 1)) * half];
           const float sdc = 0.5f * (float)packed_sign(j < 16 ? wd.x : wd.y, j & 15);
           const float sny = 0.5f * (float)packed_sign(j < 16 ? wn.x : wn.y, j & 15);
@@ -126,7 +129,7 @@ __global__ void __launch_bounds__(256, 2) k_column_w1024(const float2 *__restric
       for (int j = 0; j < 32; ++j) r[j] = make_float2(0.f, 0.f);
     }
 #pragma unroll
-    for (int j = 0; j < 32; ++j) tile[(r0 + 32 * j) * P + c] = r[j];
+    for (int j = 0; j < 32; ++j) tile[(y0 + 32 * j) * P + c] = r[j];
   }
   __syncthreads();
   float2 v[32];
@@ -142,7 +145,7 @@ __global__ void __launch_bounds__(256, 2) k_column_w1024(const float2 *__restric
   if (kx < half) {
 #pragma unroll
     for (int j = 0; j < 32; ++j) {
-      const int ky = r0 + 32 * j;
+      const int ky = y0 + 32 * j;
       out[(size_t)ky * half + kx] = tile[ky * P + c];
     }
   }
