@@ -114,12 +114,17 @@ void fill_sign_screen(SignTableArgs *a) {
   a->f_lca = (float)(a->l * a->Ca * a->inv_ps * a->inv_ps);
 }
 
-// Packed signs for the column kernels of 1024 and 4096 rows, whose threads
+// Packed signs for the column kernels of 256, 512, 1024 and 4096 rows, whose threads
 // each phase-flip rows r + R m (m < M) of one column: those M signs sit
 // together, 3 bits each (s + 2 for s in -2..2), 16 to a 64-bit word, entry
 // (d, r, kx) = M / 16 words at ((d R + r) (W/2 + 1) + kx) M / 16.  The packed
 // table follows the int8 table in the same allocation, 256-byte aligned.
 static bool sign_pack_shape(int H, int *R, int *M) {
+  if (H == 256 || H == 512) {
+    *R = H / 16;
+    *M = 16;
+    return true;
+  }
   if (H == 1024) {
     *R = 32;
     *M = 32;
@@ -181,7 +186,11 @@ cudaError_t launch_sign_pack(int8_t *sign, int D, int H, int W, cudaStream_t s) 
   unsigned long long *out = (unsigned long long *)(sign + sign_int8_bytes(D, H, W));
   const long n = (long)D * R * (W / 2 + 1);
   const int blocks = (int)std::min<long>((n + 255) / 256, 152 * 8);
-  if (H == 1024)
+  if (H == 256)
+    k_sign_pack<16, 16><<<blocks, 256, 0, s>>>(sign, D, W, out);
+  else if (H == 512)
+    k_sign_pack<32, 16><<<blocks, 256, 0, s>>>(sign, D, W, out);
+  else if (H == 1024)
     k_sign_pack<32, 32><<<blocks, 256, 0, s>>>(sign, D, W, out);
   else
     k_sign_pack<256, 16><<<blocks, 256, 0, s>>>(sign, D, W, out);

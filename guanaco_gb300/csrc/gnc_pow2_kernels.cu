@@ -1,6 +1,7 @@
-// Correction and ramp-filter kernels for power-of-two sizes (256 .. 4096; the
-// column and row stages of 1024 and 4096 use the kernels of
-// gnc_w1024_kernels.cu and gnc_b4096_kernels.cu), built on the shared-memory
+// Correction and ramp-filter kernels for power-of-two sizes: the row transform
+// of the raw projections for 256 .. 4096, the column and row stages for 2048
+// (those of 256, 512, 1024 and 4096 use the register-transform kernels of
+// gnc_w512_kernels.cu, gnc_w1024_kernels.cu and gnc_b4096_kernels.cu), built on the shared-memory
 // FFT of gnc_fft_pow2.cuh.  Same results as the generic kernels of
 // gnc_correct.cu / gnc_ramp.cu (up to float rounding), which keep serving
 // every other size.
@@ -390,9 +391,6 @@ static cudaError_t column_p2(const float2 *src, float2 *dst, const int8_t *sign,
 
 cudaError_t launch_column_fft_p2(float2 *spec, int T, int H, int W, cudaStream_t s) {
   switch (H) {
-    case 256: return column_p2<256, false>(spec, spec, nullptr, 0, T, 1, W, s);
-    case 512: return column_p2<512, false>(spec, spec, nullptr, 0, T, 1, W, s);
-    case 1024: return column_p2<1024, false>(spec, spec, nullptr, 0, T, 1, W, s);
     case 2048: return column_p2<2048, false>(spec, spec, nullptr, 0, T, 1, W, s);
   }
   return cudaErrorInvalidValue;
@@ -401,9 +399,6 @@ cudaError_t launch_column_fft_p2(float2 *spec, int T, int H, int W, cudaStream_t
 cudaError_t launch_column_flip_p2(const float2 *spec, float2 *g, const int8_t *sign, int t0,
                                   int nt, int D, int H, int W, cudaStream_t s) {
   switch (H) {
-    case 256: return column_p2<256, true>(spec, g, sign, t0, nt, D, W, s);
-    case 512: return column_p2<512, true>(spec, g, sign, t0, nt, D, W, s);
-    case 1024: return column_p2<1024, true>(spec, g, sign, t0, nt, D, W, s);
     case 2048: return column_p2<2048, true>(spec, g, sign, t0, nt, D, W, s);
   }
   return cudaErrorInvalidValue;
@@ -442,9 +437,6 @@ static cudaError_t row_p2_dispatch(const RowStageArgs &a, cudaStream_t s) {
 
 cudaError_t launch_row_stage_p2(const RowStageArgs &a, cudaStream_t s) {
   switch (a.N) {
-    case 256: return row_p2_dispatch<256>(a, s);
-    case 512: return row_p2_dispatch<512>(a, s);
-    case 1024: return row_p2_dispatch<1024>(a, s);
     case 2048: return row_p2_dispatch<2048>(a, s);
   }
   return cudaErrorInvalidValue;
