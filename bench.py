@@ -41,7 +41,7 @@ METRIC = ("3D-CTF FBP Gvoxel·tilt/s, FP16-staged vs FP32 at rel-L2≤1e-3; "
           "serve p50/p99 ms")
 UNIT = "Gvoxel·tilt/s"
 WL = dict(T=61, H=1024, W=1024, Z=300, D=10, pixel_size=1.0, defocus=30000.0, energy=300.0,
-          cs_mm=2.7, blobs=2000, seed=3, tilt_max=60.0, noise=0.1)
+          cs_mm=2.7, blobs=2000, seed=3, tilt_max=60.0, noise=0.1, ctf=True)
 WORKLOAD_NAME = ("3D CTF ndf=10: 61 tilts +-60 deg, 1024x1024 projections at 1.0 A/px, "
                  "300 kV, Cs 2.7 mm, df 30000 A, volume 1024x1024x300")
 # DRAM traffic of one k_bp_fast launch on this workload, from the ncu capture
@@ -70,6 +70,11 @@ def slab_setup():
 def make_plan(staging):
     import guanaco_gb300 as G
 
+    if not WL["ctf"]:  # plain FBP: ramp filter and backprojection only
+        c = G.get_centre((WL["T"], WL["H"], WL["W"]), None, False)
+        return G.FbpPlan(WL["T"], WL["H"], WL["W"], angles_rad(), grid_height=WL["Z"],
+                         grid_width=WL["W"], centre=c, pixel_size=WL["pixel_size"],
+                         input="raw", correct=False, staging=staging)
     c, mn, mx, step, nd = slab_setup()
     df = WL["defocus"]
     return G.FbpPlan(WL["T"], WL["H"], WL["W"], angles_rad(), grid_height=WL["Z"],
@@ -84,7 +89,8 @@ def make_projections(device):
 
     blobs = synthetic.blob_phantom(WL["blobs"], WL["W"], WL["H"], WL["Z"], WL["seed"])
     return synthetic.tilt_series(blobs, angles_rad(), WL["H"], WL["W"],
-                                 pixel_size=WL["pixel_size"], defocus=WL["defocus"],
+                                 pixel_size=WL["pixel_size"],
+                                 defocus=WL["defocus"] if WL["ctf"] else None,
                                  energy=WL["energy"], cs_mm=WL["cs_mm"], noise=WL["noise"],
                                  seed=WL["seed"], device=device)
 
@@ -260,7 +266,8 @@ def run_ours(args, rank, world, dist):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
-        "data": "synthetic: 2000-blob phantom, analytic projections through the CTF, seeded",
+        "data": (f"synthetic: {WL['blobs']}-blob phantom, analytic projections"
+                 f"{' through the CTF' if WL['ctf'] else ''}, seeded"),
         "config": {
             "workload": WORKLOAD_NAME,
             "tilts": WL["T"], "projection": [WL["H"], WL["W"]], "volume": [WL["H"], WL["W"], WL["Z"]],
@@ -444,7 +451,10 @@ def oracle_sample(proj, vols, nrows=8):
 
     c, mn, mx, step, nd = slab_setup()
     df = WL["defocus"]
-    ctf = O.ctf_stack(WL["W"], WL["H"], WL["pixel_size"], WL["energy"], mn, nd, step, WL["cs_mm"])
+    ctf = (O.ctf_stack(WL["W"], WL["H"], WL["pixel_size"], WL["energy"], mn, nd, step,
+                       WL["cs_mm"]) if WL["ctf"] else None)
+    if ctf is None:
+        mn = mx = df
     p = proj.cpu().numpy()
     ang = angles_rad()
     y0 = WL["H"] // 2 - nrows // 2
@@ -485,9 +495,11 @@ def oracle_sample(proj, vols, nrows=8):
         "cores": threads,
         "kind": "port",
         "sample": (f"oracle restatement of the reference CPU path (float, OpenMP, {threads} "
-                   f"threads): CTF correction of all {WL['T']} tilts ({t_corr:.2f} s) plus "
-                   f"filter and backprojection of {nrows} of {WL['H']} rows ({t_rows:.2f} s), "
-                   f"extrapolated to all rows: {full_s:.1f} s per series"),
+                   f"threads): "
+                   + (f"CTF correction of all {WL['T']} tilts ({t_corr:.2f} s) plus "
+                      if WL["ctf"] else "")
+                   + f"filter and backprojection of {nrows} of {WL['H']} rows ({t_rows:.2f} s), "
+                   f"extrapolated to all rows: {full_s:.2f} s per series"),
     }
     return parity, cpu
 
@@ -506,7 +518,10 @@ def run_reference(args, rank, world):
     # the sample needs only its tilts and rows: a seeded stand-in with the
     # workload's shape (the timing does not depend on the values)
     p = rng.standard_normal((WL["T"], WL["H"], WL["W"])).astype(np.float32)
-    ctf = O.ctf_stack(WL["W"], WL["H"], WL["pixel_size"], WL["energy"], mn, nd, step, WL["cs_mm"])
+    ctf = (O.ctf_stack(WL["W"], WL["H"], WL["pixel_size"], WL["energy"], mn, nd, step,
+                       WL["cs_mm"]) if WL["ctf"] else None)
+    if ctf is None:
+        mn = mx = df
     ang = angles_rad()
     k_tilts = min(WL["T"], threads)
     m_rows = threads
@@ -555,13 +570,18 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the oracle parity/CPU sample")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving stream")
-    ap.add_argument("--case", choices=["3dctf", "profile", "large", "large_profile"],
+    ap.add_argument("--case", choices=["3dctf", "profile", "large", "large_profile",
+                                       "plain_256", "single_defocus_512"],
                     default="3dctf",
                     help="profile: the same 1024^2 ndf=10 kernels on 16 tilts and a 64-voxel-"
                          "thick volume, small enough for ncu captures (not a bench line); "
                          "large: 4096^2 projections, ndf=20, 4096x4096x512 volume in one "
                          "HBM pass; large_profile: the 4096^2 kernels on 2 tilts, ndf=10 and "
-                         "a 16-voxel-thick volume, for ncu captures (not a bench line)")
+                         "a 16-voxel-thick volume, for ncu captures (not a bench line); "
+                         "plain_256: FBP without CTF, 61 tilts of 256^2 (step 2 deg), "
+                         "256x256x128 volume; single_defocus_512: CTF phase flip, one defocus "
+                         "(20000 A), 41 tilts of 512^2 (step 3 deg) at 1.35 A/px, "
+                         "512x512x256 volume")
     args = ap.parse_args()
     global WORKLOAD_NAME
     if args.case == "large":
@@ -570,6 +590,20 @@ def main():
         WORKLOAD_NAME = ("large 3D CTF ndf=20: 61 tilts +-60 deg, 4096x4096 projections at "
                          "0.8 A/px, 300 kV, Cs 2.7 mm, df 40000 A, volume 4096x4096x512")
         args.no_cpu = True
+        args.no_serve = True
+    if args.case == "plain_256":
+        WL.update(T=61, H=256, W=256, Z=128, D=1, pixel_size=1.0, blobs=200, noise=0.05,
+                  seed=0, ctf=False)
+        WORKLOAD_NAME = ("plain FBP, no CTF: 61 tilts +-60 deg (2 deg steps), 256x256 projections "
+                         "at 1.0 A/px, volume 256x256x128")
+        args.no_serve = True
+    if args.case == "single_defocus_512":
+        WL.update(T=41, H=512, W=512, Z=256, D=1, pixel_size=1.35, defocus=20000.0, blobs=500,
+                  noise=0.1, seed=1)
+        WORKLOAD_NAME = ("single-defocus CTF phase flip: 41 tilts +-60 deg (3 deg steps), "
+                         "512x512 projections at 1.35 A/px, 300 kV, Cs 2.7 mm, df 20000 A "
+                         "(amplitude contrast not modelled: the phase flip uses the sign of "
+                         "the phase-only CTF), volume 512x512x256")
         args.no_serve = True
     if args.case == "large_profile":
         WL.update(T=2, H=4096, W=4096, Z=16, D=10, pixel_size=0.8, defocus=40000.0,

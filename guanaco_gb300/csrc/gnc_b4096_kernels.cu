@@ -245,12 +245,7 @@ static cudaError_t column_b4096(const float2 *src, float2 *dst, const int8_t *si
   if (!make_fft_plan(kN, &p)) return cudaErrorInvalidValue;
   constexpr int C = kColC;
   const size_t smem = (size_t)C * kB4096Stride * sizeof(float2);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_column_b4096<FLIP, C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
-    attr = true;
-  }
+  if (cudaError_t e_attr = ensure_dynamic_smem<k_column_b4096<FLIP, C>>((int)smem)) return e_attr;
   const int half = W / 2;
   dim3 grid((half + C - 1) / C, FLIP ? D : 1, nt);
   const unsigned long long *packed = FLIP ? sign_packed(sign, D, kN, W) : nullptr;
@@ -274,11 +269,7 @@ static cudaError_t row_b4096(const RowStageArgs &a, cudaStream_t s) {
   if (!make_fft_plan(kN, &pN) || !make_fft_plan(2 * kN, &p2N)) return cudaErrorInvalidValue;
   const size_t smem = 2 * (size_t)kB4096Slots * sizeof(float2);
   auto kern = k_row_b4096<SPECTRA, RAMP, STAGED, F16>;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr = true;
-  }
+  if (cudaError_t e_attr = ensure_dynamic_smem<k_row_b4096<SPECTRA, RAMP, STAGED, F16>>((int)smem)) return e_attr;
   const long npairs = (long)a.nt * a.D * row_pairs(a);
   if (npairs == 0) return cudaSuccess;
   kern<<<(unsigned)npairs, 256, smem, s>>>(a, pN.roots, p2N.roots);

@@ -475,11 +475,7 @@ template <int RP, int KMAX, int G, bool F16>
 static cudaError_t launch_fast(const BpArgs &a, cudaStream_t s) {
   using P = FastBp<RP, KMAX, G, F16>;
   auto kern = k_bp_fast<RP, KMAX, G, F16>;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM);
-    attr = true;
-  }
+  if (cudaError_t e_attr = ensure_dynamic_smem<k_bp_fast<RP, KMAX, G, F16>>((int)P::SMEM)) return e_attr;
   const int Y2 = (a.Y + 1) / 2;
   dim3 grid((a.X + P::TX - 1) / P::TX, (a.Z + P::TZ - 1) / P::TZ, (Y2 + RP - 1) / RP);
   kern<<<grid, P::NT, P::SMEM, s>>>(a);

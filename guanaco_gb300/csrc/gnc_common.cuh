@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <string>
 
 #include "gnc_fft.cuh"
@@ -127,6 +128,22 @@ struct RowStageArgs {
   float *out_rows;       // plain rows: (nt, D, H, N) at [t][d][y][n]
 };
 cudaError_t launch_row_stage(const RowStageArgs &a, cudaStream_t s);
+
+// Raises a kernel's dynamic shared-memory limit once per device: the
+// attribute belongs to the current device's context, so a process that
+// launches on several GPUs sets it on each (one flag bit per device ordinal).
+template <auto KERNEL>
+inline cudaError_t ensure_dynamic_smem(int bytes) {
+  static std::atomic<unsigned long long> done{0ull};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (done.load(std::memory_order_acquire) & bit) return cudaSuccess;
+  e = cudaFuncSetAttribute(KERNEL, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) done.fetch_or(bit, std::memory_order_release);
+  return e;
+}
 // Row pairs a row-stage launch covers: rows 2 y2_begin .. of every (tilt, slab).
 __host__ __device__ inline int row_pairs(const RowStageArgs &a) {
   return a.y2_count > 0 ? a.y2_count : (a.H + 1) / 2;

@@ -75,11 +75,7 @@ cudaError_t launch_rfft_rows(const float *proj, float2 *spec, int T, int H, int 
   int npair = (H + 1) / 2;
   if (ppb > npair) ppb = npair;
   size_t smem = 2ull * ppb * W * sizeof(float2);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_rfft_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr_set = true;
-  }
+  if (cudaError_t e_attr = ensure_dynamic_smem<k_rfft_rows>(200 * 1024)) return e_attr;
   dim3 grid((npair + ppb - 1) / ppb, T);
   k_rfft_rows<<<grid, 256, smem, s>>>(proj, spec, H, W, ppb, plan);
   return cudaGetLastError();
@@ -134,11 +130,7 @@ cudaError_t launch_column_fft(float2 *spec, int T, int H, int W, cudaStream_t s)
   int C = column_tile(H);
   if (C > half) C = half;
   size_t smem = 2ull * H * C * sizeof(float2);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_column_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr_set = true;
-  }
+  if (cudaError_t e_attr = ensure_dynamic_smem<k_column_fft>(200 * 1024)) return e_attr;
   dim3 grid((half + C - 1) / C, T);
   k_column_fft<<<grid, 256, smem, s>>>(spec, H, W, C, plan);
   return cudaGetLastError();
@@ -199,11 +191,7 @@ cudaError_t launch_column_flip(const float2 *spec, float2 *g, const int8_t *sign
   int C = column_tile(H);
   if (C > half) C = half;
   size_t smem = 2ull * H * C * sizeof(float2);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_column_flip, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr_set = true;
-  }
+  if (cudaError_t e_attr = ensure_dynamic_smem<k_column_flip>(200 * 1024)) return e_attr;
   dim3 grid((half + C - 1) / C, D, nt);
   k_column_flip<<<grid, 256, smem, s>>>(spec, g, sign, t0, D, H, W, C, plan);
   return cudaGetLastError();

@@ -233,14 +233,11 @@ extern "C" int gnc_reconstruct_device_noalloc(const gnc_config *c, const float *
     const int npair = (nrows + 1) / 2;
     if (rp > npair) rp = npair;
     const size_t smem = 2ull * rp * L * sizeof(float2);
-    static bool attr = false;
-    if (!attr) {
-      cudaFuncSetAttribute(k_noalloc_ramp, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           200 * 1024);
-      attr = true;
+    e = ensure_dynamic_smem<k_noalloc_ramp>(200 * 1024);
+    if (e == cudaSuccess) {
+      k_noalloc_ramp<<<(npair + rp - 1) / rp, 256, smem, strm>>>(s.sino, nrows, N, plan, rp);
+      e = cudaGetLastError();
     }
-    k_noalloc_ramp<<<(npair + rp - 1) / rp, 256, smem, strm>>>(s.sino, nrows, N, plan, rp);
-    e = cudaGetLastError();
   }
   if (e == cudaSuccess) {
     SliceBpArgs a{};

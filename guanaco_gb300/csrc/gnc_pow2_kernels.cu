@@ -377,12 +377,7 @@ static cudaError_t column_p2(const float2 *src, float2 *dst, const int8_t *sign,
   FftPlan p;
   if (!make_fft_plan(H, &p)) return cudaErrorInvalidValue;
   using CT = ColTile<H>;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_column_p2<H, FLIP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)CT::SMEM);
-    attr = true;
-  }
+  if (cudaError_t e_attr = ensure_dynamic_smem<k_column_p2<H, FLIP>>((int)CT::SMEM)) return e_attr;
   const int half = W / 2;
   dim3 grid((half + CT::C - 1) / CT::C, FLIP ? D : 1, nt);
   k_column_p2<H, FLIP><<<grid, CT::THREADS, CT::SMEM, s>>>(src, dst, sign, t0, D, W, p.roots);
@@ -412,11 +407,7 @@ static cudaError_t row_p2(const RowStageArgs &a, cudaStream_t s) {
   constexpr int NB = RAMP ? 2 : 1;
   const size_t smem = (size_t)GPB * NB * Pow2<N>::PADDED * sizeof(float2);
   auto kern = k_row_p2<N, SPECTRA, RAMP, STAGED, F16>;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr = true;
-  }
+  if (cudaError_t e_attr = ensure_dynamic_smem<k_row_p2<N, SPECTRA, RAMP, STAGED, F16>>((int)smem)) return e_attr;
   const long npairs = (long)a.nt * a.D * row_pairs(a);
   kern<<<(unsigned)((npairs + GPB - 1) / GPB), 256, smem, s>>>(a, pN.roots, p2N.roots);
   return cudaGetLastError();

@@ -177,11 +177,7 @@ static cudaError_t launch_variant(const RowStageArgs &a, cudaStream_t s) {
   if (rp < 1) rp = 1;
   size_t smem = 2ull * rp * L * sizeof(float2);
   auto kern = k_row_stage<SPECTRA, RAMP, STAGED, F16>;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr_set = true;
-  }
+  if (cudaError_t e_attr = ensure_dynamic_smem<k_row_stage<SPECTRA, RAMP, STAGED, F16>>(200 * 1024)) return e_attr;
   long blocks = (npairs + rp - 1) / rp;
   kern<<<(unsigned)blocks, 256, smem, s>>>(a, pN, p2N, rp);
   return cudaGetLastError();

@@ -352,12 +352,7 @@ cudaError_t launch_rfft_rows_w1024(const float *proj, float2 *spec, int T, int H
   if (!roots_for(kN, &roots)) return cudaErrorInvalidValue;
   const int npair = (H + 1) / 2;
   const size_t smem = (1024 + 8 * kWarpFftSlots) * sizeof(float2);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_rfft_rows_w1024, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
-    attr = true;
-  }
+  if (cudaError_t e_attr = ensure_dynamic_smem<k_rfft_rows_w1024>((int)smem)) return e_attr;
   dim3 grid((npair + 7) / 8, T);
   k_rfft_rows_w1024<<<grid, 256, smem, s>>>(proj, spec, H, roots);
   return cudaGetLastError();
@@ -369,12 +364,7 @@ static cudaError_t column_w1024(const float2 *src, float2 *dst, const int8_t *si
   const float2 *roots;
   if (!roots_for(kN, &roots)) return cudaErrorInvalidValue;
   const size_t smem = (1024 + (size_t)kWarpFftSlots * 9) * sizeof(float2);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_column_w1024<FLIP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
-    attr = true;
-  }
+  if (cudaError_t e_attr = ensure_dynamic_smem<k_column_w1024<FLIP>>((int)smem)) return e_attr;
   const int half = W / 2;
   const ulonglong2 *packed = FLIP ? (const ulonglong2 *)sign_packed(sign, D, kN, W) : nullptr;
   if (((uintptr_t)packed & 15) != 0) return cudaErrorMisalignedAddress;  // 16-byte loads
@@ -398,11 +388,7 @@ static cudaError_t row_w1024(const RowStageArgs &a, cudaStream_t s) {
   if (!roots_for(kN, &roots) || !roots_for(2 * kN, &roots2N)) return cudaErrorInvalidValue;
   const size_t smem = (1024 + 4 * (kWarpFftSlots + 1024)) * sizeof(float2);
   auto kern = k_row_w1024<SPECTRA, RAMP, STAGED, F16>;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr = true;
-  }
+  if (cudaError_t e_attr = ensure_dynamic_smem<k_row_w1024<SPECTRA, RAMP, STAGED, F16>>((int)smem)) return e_attr;
   const long npairs = (long)a.nt * a.D * row_pairs(a);
   kern<<<(unsigned)((npairs + 3) / 4), 128, smem, s>>>(a, roots, roots2N);
   return cudaGetLastError();

@@ -278,12 +278,7 @@ static cudaError_t column_w512(const float2 *src, float2 *dst, const int8_t *sig
   using P = ColW512<H>;
   FftPlan p;
   if (!make_fft_plan(H, &p)) return cudaErrorInvalidValue;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_column_w512<H, FLIP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)P::SMEM);
-    attr = true;
-  }
+  if (cudaError_t e_attr = ensure_dynamic_smem<k_column_w512<H, FLIP>>((int)P::SMEM)) return e_attr;
   const unsigned long long *packed = FLIP ? sign_packed(sign, D, H, W) : nullptr;
   if (((uintptr_t)packed & 7) != 0) return cudaErrorMisalignedAddress;  // 8-byte loads
   const int half = W / 2;
