@@ -68,7 +68,7 @@ cudaError_t launch_column_fft(float2 *spec, int T, int H, int W, cudaStream_t s)
 // g (nt, D, H, W/2).
 // sign: (D, H, W/2 + 1) int8 holding 2 * (s(k) + s(-k)) / 2.
 // Bytes of a sign table allocation for (D, H, W): the int8 table (D, H, W/2+1)
-// and, for 256, 512, 1024 and 4096 rows, the packed copy the column kernels of those
+// and, for 128, 256, 384, 512, 1024 and 4096 rows, the packed copy the column kernels of those
 // sizes read (written by launch_sign_pack after launch_sign_table).
 size_t sign_table_bytes(int D, int H, int W);
 bool sign_pack_used(int H);
@@ -202,7 +202,7 @@ cudaError_t launch_column_fft_w1024(float2 *spec, int T, int W, cudaStream_t s);
 cudaError_t launch_column_flip_w1024(const float2 *spec, float2 *g, const int8_t *sign, int t0,
                                      int nt, int D, int W, cudaStream_t s);
 cudaError_t launch_row_stage_w1024(const RowStageArgs &a, cudaStream_t s);
-// Register-transform kernels for 256- and 512-pixel columns and rows
+// Register-transform kernels for 128-, 256-, 384- and 512-pixel columns and rows
 // (gnc_w512_kernels.cu); the launchers above prefer them for those sizes.
 cudaError_t launch_column_fft_w512(float2 *spec, int T, int H, int W, cudaStream_t s);
 cudaError_t launch_column_flip_w512(const float2 *spec, float2 *g, const int8_t *sign, int t0,

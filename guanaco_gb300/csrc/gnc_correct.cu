@@ -122,7 +122,7 @@ __global__ void k_column_fft(float2 *__restrict__ spec, int H, int W, int C, Fft
 cudaError_t launch_column_fft(float2 *spec, int T, int H, int W, cudaStream_t s) {
   if (H == 1024) return launch_column_fft_w1024(spec, T, W, s);
   if (H == 4096) return launch_column_fft_b4096(spec, T, W, s);
-  if (H == 256 || H == 512) return launch_column_fft_w512(spec, T, H, W, s);
+  if (H == 128 || H == 256 || H == 384 || H == 512) return launch_column_fft_w512(spec, T, H, W, s);
   if (pow2_fast(H)) return launch_column_fft_p2(spec, T, H, W, s);
   FftPlan plan;
   if (!make_fft_plan(H, &plan)) return cudaErrorInvalidValue;
@@ -183,7 +183,7 @@ cudaError_t launch_column_flip(const float2 *spec, float2 *g, const int8_t *sign
                                int D, int H, int W, cudaStream_t s) {
   if (H == 1024) return launch_column_flip_w1024(spec, g, sign, t0, nt, D, W, s);
   if (H == 4096) return launch_column_flip_b4096(spec, g, sign, t0, nt, D, W, s);
-  if (H == 256 || H == 512) return launch_column_flip_w512(spec, g, sign, t0, nt, D, H, W, s);
+  if (H == 128 || H == 256 || H == 384 || H == 512) return launch_column_flip_w512(spec, g, sign, t0, nt, D, H, W, s);
   if (pow2_fast(H)) return launch_column_flip_p2(spec, g, sign, t0, nt, D, H, W, s);
   FftPlan plan;
   if (!make_fft_plan(H, &plan)) return cudaErrorInvalidValue;

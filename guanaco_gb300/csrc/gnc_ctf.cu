@@ -114,15 +114,15 @@ void fill_sign_screen(SignTableArgs *a) {
   a->f_lca = (float)(a->l * a->Ca * a->inv_ps * a->inv_ps);
 }
 
-// Packed signs for the column kernels of 256, 512, 1024 and 4096 rows, whose threads
+// Packed signs for the column kernels of 128, 256, 384, 512, 1024 and 4096 rows, whose threads
 // each phase-flip rows r + R m (m < M) of one column: those M signs sit
 // together, 3 bits each (s + 2 for s in -2..2), 16 to a 64-bit word, entry
-// (d, r, kx) = M / 16 words at ((d R + r) (W/2 + 1) + kx) M / 16.  The packed
+// (d, r, kx) = ceil(M / 16) words at ((d R + r) (W/2 + 1) + kx) ceil(M / 16).  The packed
 // table follows the int8 table in the same allocation, 256-byte aligned.
 static bool sign_pack_shape(int H, int *R, int *M) {
-  if (H == 256 || H == 512) {
-    *R = H / 16;
-    *M = 16;
+  if (H == 128 || H == 256 || H == 384 || H == 512) {  // the tiles of gnc_w512_kernels.cu
+    *R = H >= 384 ? 32 : (H == 256 ? 16 : 8);
+    *M = H / *R;
     return true;
   }
   if (H == 1024) {
@@ -150,7 +150,7 @@ static size_t sign_int8_bytes(int D, int H, int W) {
 size_t sign_table_bytes(int D, int H, int W) {
   int R, M;
   if (!sign_pack_shape(H, &R, &M)) return (size_t)D * H * (W / 2 + 1);
-  return sign_int8_bytes(D, H, W) + (size_t)D * R * (W / 2 + 1) * (M / 16) * 8;
+  return sign_int8_bytes(D, H, W) + (size_t)D * R * (W / 2 + 1) * ((M + 15) / 16) * 8;
 }
 
 const unsigned long long *sign_packed(const int8_t *sign, int D, int H, int W) {
@@ -160,7 +160,7 @@ const unsigned long long *sign_packed(const int8_t *sign, int D, int H, int W) {
 template <int R, int M>
 __global__ void k_sign_pack(const int8_t *__restrict__ sign, int D, int W,
                             unsigned long long *__restrict__ out) {
-  constexpr int H = R * M, NW = M / 16;
+  constexpr int H = R * M, NW = (M + 15) / 16;
   const int sw = W / 2 + 1;
   const long n = (long)D * R * sw;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -186,7 +186,11 @@ cudaError_t launch_sign_pack(int8_t *sign, int D, int H, int W, cudaStream_t s) 
   unsigned long long *out = (unsigned long long *)(sign + sign_int8_bytes(D, H, W));
   const long n = (long)D * R * (W / 2 + 1);
   const int blocks = (int)std::min<long>((n + 255) / 256, 152 * 8);
-  if (H == 256)
+  if (H == 128)
+    k_sign_pack<8, 16><<<blocks, 256, 0, s>>>(sign, D, W, out);
+  else if (H == 384)
+    k_sign_pack<32, 12><<<blocks, 256, 0, s>>>(sign, D, W, out);
+  else if (H == 256)
     k_sign_pack<16, 16><<<blocks, 256, 0, s>>>(sign, D, W, out);
   else if (H == 512)
     k_sign_pack<32, 16><<<blocks, 256, 0, s>>>(sign, D, W, out);

@@ -186,7 +186,7 @@ static cudaError_t launch_variant(const RowStageArgs &a, cudaStream_t s) {
 cudaError_t launch_row_stage(const RowStageArgs &a, cudaStream_t s) {
   if (a.N == 1024) return launch_row_stage_w1024(a, s);
   if (a.N == 4096) return launch_row_stage_b4096(a, s);
-  if (a.N == 256 || a.N == 512) return launch_row_stage_w512(a, s);
+  if (a.N == 128 || a.N == 256 || a.N == 384 || a.N == 512) return launch_row_stage_w512(a, s);
   if (pow2_fast(a.N)) return launch_row_stage_p2(a, s);
   const bool sp = a.input_spectra != 0, rm = a.ramp != 0, st = a.out_staged != 0;
   const bool h = a.staging == kStageF16;

@@ -1,7 +1,7 @@
-// Correction and ramp-filter kernels for 256- and 512-pixel rows and columns,
-// built on the register transforms of gnc_fft_w512.cuh (one warp per
-// 512-point transform, one half warp per 256-point transform, 16 values per
-// lane).  They compute what the power-of-two kernels of gnc_pow2_kernels.cu
+// Correction and ramp-filter kernels for 128-, 256-, 384- and 512-pixel rows
+// and columns, built on the register transforms of gnc_fft_w512.cuh (16
+// values per lane; a warp runs one 512- or 384-point transform, two 256-point
+// or four 128-point ones).  They compute what the power-of-two kernels of gnc_pow2_kernels.cu
 // compute (same phase flip of the packed half spectra, same four-transform
 // form of the zero-padded ramp filter, see there): the row stage chains its
 // four transforms and the pointwise products in registers and holds the even
@@ -23,16 +23,18 @@ __device__ __forceinline__ float ramp_wn(int K) {  // filter.cpp:38-41, w_K = K 
 
 __device__ __forceinline__ float2 scale2(float w, float2 v) { return make_float2(w * v.x, w * v.y); }
 
-// Column tile of the 512- and 256-row column kernels: C columns, row pitch P
-// (float2).  512 rows: 8 columns (64-byte row pieces), one warp per column,
-// rows of a thread y0 + 32 j with y0 permuting the 32 residues so that the two
-// rows of a half warp are 8 apart (pitch 9: bank pairs 0-7 and 8-15).  256
-// rows: 16 columns (128-byte row pieces), one half warp per column, rows
-// r0 + 16 j (a half warp covers one row piece).
+// Column tile of the column kernels: C columns, row pitch P (float2), one
+// transform per column.  512 and 384 rows: 8 columns (64-byte row pieces), a
+// warp per column, rows of a thread y0 + 32 j with y0 permuting the 32
+// residues so that the two rows of a half warp are 8 apart (pitch 9: bank
+// pairs 0-7 and 8-15).  256 rows: 16 columns (128-byte row pieces), a half warp
+// per column.  128 rows: 32 columns (256-byte row pieces), a quarter warp per
+// column, pitch 34 (= 2 mod 16) so that the two columns of a half warp read
+// distinct bank pairs.
 template <int H>
 struct ColW512 {
-  static constexpr int C = H == 512 ? 8 : 16;
-  static constexpr int P = C + 1;
+  static constexpr int C = H >= 384 ? 8 : (H == 256 ? 16 : 32);
+  static constexpr int P = H == 128 ? 34 : C + 1;
   static constexpr int RS = 256 / C;  // row residues per pass of the block
   static constexpr int J = H / RS;    // rows per thread
   static constexpr int SLOTS = WarpFftShape<H>::SLOTS;
@@ -65,7 +67,7 @@ __global__ void __launch_bounds__(256, 3) k_column_w512(const float2 *__restrict
   const float2 *F = src + (size_t)t * H * half;
   const int sw = half + 1;
   const int c = threadIdx.x % C, r0 = threadIdx.x / C;
-  const int y0 = H == 512 ? (r0 & 16) + ((r0 >> 1) & 7) + 8 * (r0 & 1) : r0;
+  const int y0 = C == 8 ? (r0 & 16) + ((r0 >> 1) & 7) + 8 * (r0 & 1) : r0;
   const int kx = c0 + c;
   {
     float2 r[P::J];
@@ -79,7 +81,7 @@ __global__ void __launch_bounds__(256, 3) k_column_w512(const float2 *__restrict
 #pragma unroll
           for (int j = 0; j < P::J; ++j) {
             const int ky = y0 + P::RS * j;
-            const float2 m = F[(size_t)((H - ky) & (H - 1)) * half];
+            const float2 m = F[(size_t)(ky == 0 ? 0 : H - ky) * half];  // row -ky mod H
             const float sdc = 0.5f * (float)packed_sign(wd, j);
             const float sny = 0.5f * (float)packed_sign(wn, j);
             const float a = 0.5f * (sdc + sny), b = 0.5f * (sdc - sny);
@@ -100,15 +102,21 @@ __global__ void __launch_bounds__(256, 3) k_column_w512(const float2 *__restrict
   }
   __syncthreads();
   {
+    constexpr int TPW = WarpFftShape<H>::TPW;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int ct = w * (32 / L) + lane / L, l = lane % L;  // this transform's column
+    const int sub = lane / L;
+    const bool act = sub < TPW;  // 384 rows: lanes 24..31 idle
+    const int l = act ? lane % L : lane - TPW * L;
+    const int ct = w * TPW + (act ? sub : 0);  // this transform's column
     float2 *slots = tile + (size_t)H * P::P + (size_t)ct * P::SLOTS;
     float2 v[16];
 #pragma unroll
-    for (int m = 0; m < 16; ++m) v[m] = tile[(l + L * m) * P::P + ct];
-    warp_fft_n<H, FLIP>(v, slots, roots, l);
+    for (int m = 0; m < 16; ++m) v[m] = act ? tile[(l + L * m) * P::P + ct] : make_float2(0.f, 0.f);
+    warp_fft_n<H, FLIP>(v, slots, roots, l, act);
+    if (act) {
 #pragma unroll
-    for (int m = 0; m < 16; ++m) tile[(l + L * m) * P::P + ct] = v[m];
+      for (int m = 0; m < 16; ++m) tile[(l + L * m) * P::P + ct] = v[m];
+    }
   }
   __syncthreads();
   float2 *out = FLIP ? dst + ((size_t)tl * D + d) * H * half : dst + (size_t)t * H * half;
@@ -122,8 +130,9 @@ __global__ void __launch_bounds__(256, 3) k_column_w512(const float2 *__restrict
 }
 
 // ---------------------------------------------------------------------------
-// Row stage for 256- and 512-pixel rows: one transform group (a warp for 512,
-// a half warp for 256) per row pair, four warps per block.
+// Row stage for 128-, 256-, 384- and 512-pixel rows: one transform (a warp for
+// 512 and 384, a half or quarter warp for 256 and 128) per row pair, four
+// warps per block.
 // SPECTRA + RAMP: u = IFFT(w_even Z) is held in registers while the odd path
 // c = IFFT(Z), c exp(-i pi n/N), FFT, times w_odd, IFFT runs; then u's
 // transform.  Rows + RAMP: the twisted rows are held while the even path runs.
@@ -132,16 +141,18 @@ template <int N, bool SPECTRA, bool RAMP, bool STAGED, bool F16>
 __global__ void __launch_bounds__(128) k_row_w512(RowStageArgs a, const float2 *__restrict__ roots,
                                                   const float2 *__restrict__ roots2N) {
   using S = WarpFftShape<N>;
-  constexpr int L = S::L, TPW = 32 / L, PPB = 4 * TPW;
+  constexpr int L = S::L, TPW = S::TPW, PPB = 4 * TPW;
   __shared__ float2 slots_all[PPB][S::SLOTS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int sub = lane / L, l = lane % L;
+  // 384: lanes 24..31 are idle and shadow lanes 0..7 (same loads, no stores)
+  const bool act = lane / L < TPW;
+  const int sub = act ? lane / L : 0, l = act ? lane % L : lane - TPW * L;
   float2 *slots = slots_all[w * TPW + sub];
   const int Y2 = row_pairs(a);  // row pairs of this launch
   const long npairs = (long)a.nt * a.D * Y2;
   long pair = (long)blockIdx.x * PPB + w * TPW + sub;
-  const bool active = pair < npairs;
-  if (!active) pair = npairs - 1;  // the lanes of a warp stay together for its shuffles
+  const bool active = act && pair < npairs;
+  if (pair >= npairs) pair = npairs - 1;  // the lanes of a warp stay together for its shuffles
   const int tl = (int)(pair / ((long)a.D * Y2));
   const int rem = (int)(pair - (long)tl * a.D * Y2);
   const int d = rem / Y2, y2 = a.y2_begin + (rem - d * Y2);
@@ -170,7 +181,7 @@ __global__ void __launch_bounds__(128) k_row_w512(RowStageArgs a, const float2 *
       }
       if (RAMP) u[m] = scale2(ramp_wn<N>(2 * k), o[m]);
     }
-    warp_fft_n<N, true>(o, slots, roots, l);  // c = IFFT(Z)
+    warp_fft_n<N, true>(o, slots, roots, l, act);  // c = IFFT(Z)
   } else {
     const float *ra = a.rows + ((size_t)(a.t0 + tl) * a.D + d) * a.plane_stride +
                       (size_t)ya * a.row_stride;
@@ -183,7 +194,7 @@ __global__ void __launch_bounds__(128) k_row_w512(RowStageArgs a, const float2 *
     if (RAMP) {
 #pragma unroll
       for (int m = 0; m < 16; ++m) o[m] = u[m];
-      warp_fft_n<N, false>(u, slots, roots, l);  // FFT(c)
+      warp_fft_n<N, false>(u, slots, roots, l, act);  // FFT(c)
 #pragma unroll
       for (int m = 0; m < 16; ++m) u[m] = scale2(ramp_wn<N>(2 * (l + L * m)), u[m]);
     }
@@ -192,11 +203,11 @@ __global__ void __launch_bounds__(128) k_row_w512(RowStageArgs a, const float2 *
     // odd bins: FFT(c exp(-i pi n / N)), times w_odd, inverse
 #pragma unroll
     for (int m = 0; m < 16; ++m) o[m] = cmul(o[m], __ldg(roots2N + l + L * m));
-    warp_fft_n<N, false>(o, slots, roots, l);
+    warp_fft_n<N, false>(o, slots, roots, l, act);
 #pragma unroll
     for (int m = 0; m < 16; ++m) o[m] = scale2(ramp_wn<N>(2 * (l + L * m) + 1), o[m]);
-    warp_fft_n<N, true>(o, slots, roots, l);
-    warp_fft_n<N, true>(u, slots, roots, l);  // the even path
+    warp_fft_n<N, true>(o, slots, roots, l, act);
+    warp_fft_n<N, true>(u, slots, roots, l, act);  // the even path
   }
 
   // ---- combine and write
@@ -228,8 +239,11 @@ __global__ void __launch_bounds__(128) k_row_w512(RowStageArgs a, const float2 *
       ma = fmaxf(ma, fabsf(yv[m].x));
       mb = fmaxf(mb, fabsf(yv[m].y));
     }
+    if (!act) ma = mb = 0.f;
+    // within the transform's lanes (384: the whole warp, idle lanes at 0)
+    constexpr int R0 = (L & (L - 1)) ? 16 : L / 2;
 #pragma unroll
-    for (int off = L / 2; off > 0; off >>= 1) {  // within the transform's lanes
+    for (int off = R0; off > 0; off >>= 1) {
       ma = fmaxf(ma, __shfl_xor_sync(0xffffffffu, ma, off));
       mb = fmaxf(mb, __shfl_xor_sync(0xffffffffu, mb, off));
     }
@@ -244,7 +258,7 @@ __global__ void __launch_bounds__(128) k_row_w512(RowStageArgs a, const float2 *
     for (int m = 0; m < 16; ++m) yv[m] = make_float2(yv[m].x * sa, yv[m].y * sb);
     // pixel n + 1 of n = l + L m: lane l + 1's element m, or lane 0's element
     // m + 1 for l = L - 1 (the last pixel is its own neighbour)
-    const int nb_lane = sub * L + ((l + 1) & (L - 1));
+    const int nb_lane = sub * L + (l + 1) % L;
     const size_t rowi = ((size_t)y2 * a.D + d) * a.T + t;
     uint2 *dst = (uint2 *)a.staged + rowi * N;
 #pragma unroll
@@ -288,15 +302,23 @@ static cudaError_t column_w512(const float2 *src, float2 *dst, const int8_t *sig
 }
 
 cudaError_t launch_column_fft_w512(float2 *spec, int T, int H, int W, cudaStream_t s) {
-  if (H == 512) return column_w512<512, false>(spec, spec, nullptr, 0, T, 1, W, s);
-  if (H == 256) return column_w512<256, false>(spec, spec, nullptr, 0, T, 1, W, s);
+  switch (H) {
+    case 128: return column_w512<128, false>(spec, spec, nullptr, 0, T, 1, W, s);
+    case 256: return column_w512<256, false>(spec, spec, nullptr, 0, T, 1, W, s);
+    case 384: return column_w512<384, false>(spec, spec, nullptr, 0, T, 1, W, s);
+    case 512: return column_w512<512, false>(spec, spec, nullptr, 0, T, 1, W, s);
+  }
   return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_column_flip_w512(const float2 *spec, float2 *g, const int8_t *sign, int t0,
                                     int nt, int D, int H, int W, cudaStream_t s) {
-  if (H == 512) return column_w512<512, true>(spec, g, sign, t0, nt, D, W, s);
-  if (H == 256) return column_w512<256, true>(spec, g, sign, t0, nt, D, W, s);
+  switch (H) {
+    case 128: return column_w512<128, true>(spec, g, sign, t0, nt, D, W, s);
+    case 256: return column_w512<256, true>(spec, g, sign, t0, nt, D, W, s);
+    case 384: return column_w512<384, true>(spec, g, sign, t0, nt, D, W, s);
+    case 512: return column_w512<512, true>(spec, g, sign, t0, nt, D, W, s);
+  }
   return cudaErrorInvalidValue;
 }
 
@@ -304,7 +326,7 @@ template <int N, bool SPECTRA, bool RAMP, bool STAGED, bool F16>
 static cudaError_t row_w512(const RowStageArgs &a, cudaStream_t s) {
   FftPlan pN, p2N;
   if (!make_fft_plan(N, &pN) || !make_fft_plan(2 * N, &p2N)) return cudaErrorInvalidValue;
-  constexpr int PPB = 4 * (32 / WarpFftShape<N>::L);
+  constexpr int PPB = 4 * WarpFftShape<N>::TPW;
   const long npairs = (long)a.nt * a.D * row_pairs(a);
   if (npairs == 0) return cudaSuccess;
   k_row_w512<N, SPECTRA, RAMP, STAGED, F16><<<(unsigned)((npairs + PPB - 1) / PPB), 128, 0, s>>>(
@@ -326,8 +348,12 @@ static cudaError_t row_w512_dispatch(const RowStageArgs &a, cudaStream_t s) {
 }
 
 cudaError_t launch_row_stage_w512(const RowStageArgs &a, cudaStream_t s) {
-  if (a.N == 512) return row_w512_dispatch<512>(a, s);
-  if (a.N == 256) return row_w512_dispatch<256>(a, s);
+  switch (a.N) {
+    case 128: return row_w512_dispatch<128>(a, s);
+    case 256: return row_w512_dispatch<256>(a, s);
+    case 384: return row_w512_dispatch<384>(a, s);
+    case 512: return row_w512_dispatch<512>(a, s);
+  }
   return cudaErrorInvalidValue;
 }
 

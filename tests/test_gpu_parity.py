@@ -278,7 +278,8 @@ def test_pipeline_vs_oracles(torch, oracle, staging, shape):
 @pytest.mark.parametrize("T,H,W,Z,D,ragged", [(37, 64, 256, 40, 4, False), (19, 90, 128, 30, 3, True),
                                                 (9, 22, 64, 48, 1, False), (11, 45, 256, 20, 2, False),
                                                 (5, 250, 128, 16, 2, False),
-                                                (6, 1024, 1024, 24, 3, False)])
+                                                (6, 1024, 1024, 24, 3, False),
+                                                (4, 384, 384, 16, 3, False)])
 def test_host_pipeline_equals_device_path(torch, oracle, staging, T, H, W, Z, D, ragged):
     centre = None
     if ragged:  # per-row centres: the exact backprojector
@@ -372,7 +373,8 @@ def test_linearity_at_full_detector_width(torch, oracle):
 @pytest.mark.parametrize("shape", [(5, 256, 1024, 48, 3), (7, 512, 256, 64, 4),
                                    (3, 1024, 256, 32, 2), (6, 243, 512, 40, 5),
                                    (3, 2048, 256, 16, 2), (2, 4096, 128, 16, 3),
-                                   (2, 16, 4096, 16, 3)])
+                                   (2, 16, 4096, 16, 3), (4, 128, 384, 32, 3),
+                                   (3, 384, 128, 40, 2), (2, 384, 384, 24, 4)])
 def test_pipeline_pow2_sizes_vs_oracles(torch, oracle, staging, shape):
     T, H, W, Z, D = shape
     plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=T, H=H, W=W, Z=Z, D=D, staging=staging,
@@ -387,7 +389,7 @@ def test_pipeline_pow2_sizes_vs_oracles(torch, oracle, staging, shape):
         assert rel_l2(vol, ref) < FP16_TOL
 
 
-@pytest.mark.parametrize("W", [256, 512, 2048, 4096])
+@pytest.mark.parametrize("W", [128, 256, 384, 512, 2048, 4096])
 def test_plain_filter_pow2_vs_oracle(torch, oracle, W):
     """No CTF: the projections are ramp filtered and backprojected directly."""
     import guanaco_gb300 as G
@@ -409,7 +411,8 @@ def test_plain_filter_pow2_vs_oracle(torch, oracle, W):
     assert rel_l2(buf.cpu().numpy(), oracle.ramp_filter(rows)) < 1e-6
 
 
-@pytest.mark.parametrize("T,H,W,D", [(3, 256, 512, 4), (2, 16, 4096, 3), (1, 4096, 64, 2)])
+@pytest.mark.parametrize("T,H,W,D", [(3, 256, 512, 4), (2, 16, 4096, 3), (1, 4096, 64, 2),
+                                     (2, 384, 128, 3), (2, 128, 384, 2)])
 def test_correct_only_pow2(torch, oracle, T, H, W, D):
     plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=T, H=H, W=W, D=D, seed=4)
     out = torch.empty((plan.T, plan.D, plan.H, plan.W), dtype=torch.float32, device="cuda")
