@@ -1,17 +1,21 @@
 // Request server: continuous batching of whole-series FBP requests on one GPU.
 //
-// One scheduler thread owns the device work.  Callers queue requests
+// A scheduler thread admits requests.  Callers queue requests
 // (gnc_server_submit); the scheduler admits a request when a slot (a CUDA
 // stream) is free and its plan fits in the device-memory budget, and enqueues
 // on that slot: the parameter upload, the input copy, the device work and the
 // volume copy, followed by a host callback that marks the slot finished.
 // Requests on different slots overlap on the device.
 //
-// Plans are cached by shape (plan_key).  The first request of a shape runs as
-// direct launches, which also creates the FFT tables and kernel attributes the
-// launches need; the same launch sequence is then captured once as a CUDA
-// graph, and later requests of that shape replay it after uploading their own
-// parameter block (the kernels read per-request values from device memory).
+// Plans are cached by shape (plan_key).  A request with no idle plan of its
+// shape gets its slot, memory and cache entry from the scheduler and is handed
+// to a builder thread, which creates the plan, runs the request as direct
+// launches (creating the FFT tables and kernel attributes they need) and then
+// captures the same launch sequence once as a CUDA graph; meanwhile the
+// scheduler keeps admitting requests of known shapes.  Later requests of that
+// shape replay the graph after uploading their own parameter block (the
+// kernels read per-request values from device memory).  Only the builder
+// captures, on its own stream.
 //
 // Admission takes the oldest queued request that can run now; when it cannot
 // (no idle plan of its shape and not enough memory even after releasing idle
@@ -90,9 +94,16 @@ struct gnc_server {
   std::unordered_map<uint64_t, std::unique_ptr<Request>> reqs;
   std::vector<std::unique_ptr<Cached>> cache;
   std::mutex mu;
-  std::condition_variable cv_sched, cv_done;
-  std::thread th;
-  bool stop = false, wake = false;
+  std::condition_variable cv_sched, cv_done, cv_build;
+  std::thread th, th_build;
+  bool stop = false, wake = false, stop_build = false;
+  struct Build {  // a request whose new plan the builder creates
+    Slot *sl;
+    Request *r;
+    Cached *c;
+    std::vector<std::unique_ptr<Cached>> victims;  // idle plans released for its memory
+  };
+  std::deque<Build> builds;
   uint64_t next_id = 1, tick = 0;
   int head_skips = 0;
   std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
@@ -128,6 +139,12 @@ Cached *find_idle(gnc_server *S, const std::string &key) {
   for (auto &c : S->cache)
     if (c->ready && !c->busy && c->key == key) return c.get();
   return nullptr;
+}
+
+bool being_built(gnc_server *S, const std::string &key) {
+  for (auto &c : S->cache)
+    if (!c->ready && c->key == key) return true;
+  return false;
 }
 
 size_t idle_bytes(gnc_server *S) {
@@ -200,8 +217,9 @@ void capture(gnc_server *S, Cached *c) {
   cudaGetLastError();  // a failed capture leaves direct launches in use
 }
 
-// Without the lock: everything one request puts on its slot's stream.
-int enqueue(gnc_server *S, Slot *sl, Request *r, Cached *c, bool *captured_now) {
+// Without the lock: everything one request puts on its slot's stream; with
+// may_capture (the builder), a plan without a graph captures one afterwards.
+int enqueue(gnc_server *S, Slot *sl, Request *r, Cached *c, bool may_capture) {
   cudaStream_t s = sl->s;
   int st = gnc::plan_set_request(c->plan, &r->desc, c->h_params, s);
   if (st != GNC_OK) return st;
@@ -225,10 +243,7 @@ int enqueue(gnc_server *S, Slot *sl, Request *r, Cached *c, bool *captured_now) 
     gnc::set_error(std::string("gnc_server: ") + cudaGetErrorString(e));
     return GNC_ERR_CUDA;
   }
-  if (!c->exec) {
-    capture(S, c);
-    *captured_now = true;
-  }
+  if (may_capture && !c->exec) capture(S, c);
   return GNC_OK;
 }
 
@@ -250,6 +265,8 @@ void admit(gnc_server *S, std::unique_lock<std::mutex> &lk) {
       if (qi > 0 && S->head_skips >= kMaxSkips) break;
       Request *q = S->queue[qi];
       c = find_idle(S, q->key);
+      // a shape whose plan the builder is making waits for it (no second copy)
+      if (!c && being_built(S, q->key)) continue;
       if (c || S->used - idle + q->bytes <= S->budget) {
         r = q;
         break;
@@ -289,30 +306,19 @@ void admit(gnc_server *S, std::unique_lock<std::mutex> &lk) {
     r->t_start = S->now();
     S->st.in_flight++;
     S->st.peak_in_flight = std::max(S->st.peak_in_flight, S->st.in_flight);
+    if (fresh) {  // the builder creates the plan and runs the request
+      S->builds.push_back(gnc_server::Build{sl, r, c, std::move(victims)});
+      S->cv_build.notify_one();
+      continue;
+    }
     lk.unlock();
-    for (auto &v : victims) release(v.get());
-    int st = GNC_OK;
     std::string msg;
-    if (fresh) {
-      st = create_entry(S, c, r);
-      if (st != GNC_OK) msg = gnc::last_error();
-    }
-    bool captured_now = false;
     const bool replay = c->exec != nullptr;
-    if (st == GNC_OK) {
-      st = enqueue(S, sl, r, c, &captured_now);
-      if (st != GNC_OK) msg = gnc::last_error();
-    }
-    if (st != GNC_OK && fresh) release(c);
+    int st = enqueue(S, sl, r, c, false);
+    if (st != GNC_OK) msg = gnc::last_error();
     lk.lock();
     if (st != GNC_OK) {
-      if (fresh) {
-        S->used -= c->bytes;
-        S->cache.erase(std::find_if(S->cache.begin(), S->cache.end(),
-                                    [c](const std::unique_ptr<Cached> &p) { return p.get() == c; }));
-      } else {
-        c->busy = false;
-      }
+      c->busy = false;
       sl->req = nullptr;
       sl->plan = nullptr;
       S->st.in_flight--;
@@ -320,14 +326,53 @@ void admit(gnc_server *S, std::unique_lock<std::mutex> &lk) {
       S->cv_done.notify_all();
       continue;
     }
-    if (fresh) {
-      c->ready = true;
-      S->st.plans_created++;
-    }
     if (replay)
       S->st.graph_launches++;
     else
       S->st.direct_launches++;
+  }
+}
+
+// The builder thread: new plans, their first (direct) run and their capture.
+void build_loop(gnc_server *S) {
+  cudaSetDevice(S->device);
+  std::unique_lock<std::mutex> lk(S->mu);
+  for (;;) {
+    S->cv_build.wait(lk, [S] { return S->stop_build || !S->builds.empty(); });
+    if (S->builds.empty()) break;  // stop_build and nothing left
+    gnc_server::Build b = std::move(S->builds.front());
+    S->builds.pop_front();
+    lk.unlock();
+    for (auto &v : b.victims) release(v.get());
+    b.victims.clear();
+    std::string msg;
+    int st = create_entry(S, b.c, b.r);
+    if (st != GNC_OK) msg = gnc::last_error();
+    if (st == GNC_OK) {
+      st = enqueue(S, b.sl, b.r, b.c, true);
+      if (st != GNC_OK) msg = gnc::last_error();
+    }
+    if (st != GNC_OK) release(b.c);
+    lk.lock();
+    if (st != GNC_OK) {
+      S->used -= b.c->bytes;
+      Cached *c = b.c;
+      S->cache.erase(std::find_if(S->cache.begin(), S->cache.end(),
+                                  [c](const std::unique_ptr<Cached> &p) { return p.get() == c; }));
+      b.sl->req = nullptr;
+      b.sl->plan = nullptr;
+      S->st.in_flight--;
+      fail(S, b.r, st, msg);
+      S->cv_done.notify_all();
+      S->wake = true;  // the slot and the memory are free again
+      S->cv_sched.notify_one();
+      continue;
+    }
+    b.c->ready = true;
+    S->st.plans_created++;
+    S->st.direct_launches++;
+    S->wake = true;  // requests that waited for this shape can be admitted
+    S->cv_sched.notify_one();
   }
 }
 
@@ -389,6 +434,7 @@ int gnc_server_create(size_t budget_bytes, int slots, gnc_server **server) {
   S->st.slots = slots;
   gnc_server *raw = S.release();
   raw->th = std::thread(run, raw);
+  raw->th_build = std::thread(build_loop, raw);
   *server = raw;
   return GNC_OK;
 }
@@ -404,7 +450,13 @@ int gnc_server_destroy(gnc_server *S) {
     S->cv_sched.notify_one();
     S->cv_done.notify_all();
   }
-  S->th.join();
+  S->th.join();  // returns once every slot, those being built included, is done
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stop_build = true;
+    S->cv_build.notify_one();
+  }
+  S->th_build.join();
   cudaSetDevice(S->device);
   for (Slot &sl : S->slots) cudaStreamSynchronize(sl.s);
   for (auto &c : S->cache) release(c.get());
