@@ -357,6 +357,9 @@ k_bp_fast(BpArgs a) {
         issue_copies(tg + G, min(G, nch - tg - G), tbase, b ^ 1);
       if (!F16) land(grp, gg);
       const unsigned char *buf = smem_raw + b * P::BUF;
+      // FP32: two tilts unrolled, so one tilt's loads overlap the other's sums
+      constexpr int kUnrollTilts = F16 ? 1 : 2;
+#pragma unroll kUnrollTilts
       for (int gi = 0; gi < ng; ++gi) {
         const TiltParams tp = s_tp[tg + gi];
         float xc[A], zs[B];
