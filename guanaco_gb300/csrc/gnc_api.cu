@@ -629,7 +629,10 @@ static int execute_host_pipelined(gnc_fbp_plan *p, const float *h_input, float *
   GNC_CUDA(cudaEventRecord(ev_start, s));
   GNC_CUDA(cudaStreamWaitEvent(p->s_in, ev_start, 0));
   GNC_CUDA(cudaStreamWaitEvent(p->s_out, ev_start, 0));
-  const int group = std::max(8, (p->T + kIoGroups - 1) / kIoGroups);
+  // tilt groups of at least 8 tilts and 8 MB (small series: fewer, larger copies)
+  const size_t tilt_bytes = per_tilt * sizeof(float);
+  const int group = std::max({8, (p->T + kIoGroups - 1) / kIoGroups,
+                              (int)((((size_t)8 << 20) + tilt_bytes - 1) / tilt_bytes)});
   for (int g = 0, t0 = 0; t0 < p->T; ++g, t0 += group) {
     const int n = std::min(group, p->T - t0);
     GNC_CUDA(cudaMemcpyAsync(p->io_in + (size_t)t0 * per_tilt, h_input + (size_t)t0 * per_tilt,
@@ -683,11 +686,15 @@ static int execute_host_pipelined(gnc_fbp_plan *p, const float *h_input, float *
     r.nt = p->T;
   }
   // backprojection in slabs of whole row pairs, each copied out when done: at
-  // most 8 slabs of whole block rows, the last one split into 1/2, 1/4, 1/4
-  const int rows = ((p->H + 7) / 8 + 7) / 8 * 8;
+  // most 8 slabs of whole block rows and at least 16 MB each, the last one split
+  // into 1/2, 1/4, 1/4 when slabs are larger than that
+  const size_t row_bytes = plane * sizeof(float);
+  const size_t min_slab = (size_t)16 << 20;
+  const int rows = std::max(((p->H + 7) / 8 + 7) / 8 * 8,
+                            (int)((min_slab / row_bytes + 7) / 8 * 8));
   int slab_y0[kIoSlabs + 1], nslab = 0;
   for (int y0 = 0; y0 < p->H; y0 += rows) slab_y0[nslab++] = y0;
-  if (rows >= 32) {
+  if (rows >= 32 && (size_t)rows * row_bytes > min_slab) {
     const int last = slab_y0[nslab - 1], n_last = p->H - last;
     const int a = std::min(rows / 2, n_last), b = std::min(rows / 4, n_last - a);
     if (a < n_last) slab_y0[nslab++] = last + a;

@@ -273,12 +273,13 @@ def test_pipeline_vs_oracles(torch, oracle, staging, shape):
 # in, row slabs out; with CTF correction it filters row slab by row slab); it
 # must give exactly the device entry point's volume.  Shapes: power-of-two and
 # generic rows, an odd row count (a last slab with a single-row pair), and
-# row counts whose last slab is split in three (250 and 1024 rows).
+# 1024-pixel rows: three input groups of at least 8 MB and six volume slabs of
+# at least 16 MB, the last split in three.
 @pytest.mark.parametrize("staging", ["f32", "f16"])
 @pytest.mark.parametrize("T,H,W,Z,D,ragged", [(37, 64, 256, 40, 4, False), (19, 90, 128, 30, 3, True),
                                                 (9, 22, 64, 48, 1, False), (11, 45, 256, 20, 2, False),
                                                 (5, 250, 128, 16, 2, False),
-                                                (6, 1024, 1024, 24, 3, False),
+                                                (17, 1024, 1024, 24, 3, False),
                                                 (4, 384, 384, 16, 3, False)])
 def test_host_pipeline_equals_device_path(torch, oracle, staging, T, H, W, Z, D, ragged):
     centre = None
