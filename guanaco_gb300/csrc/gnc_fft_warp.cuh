@@ -147,34 +147,6 @@ __device__ __forceinline__ void dft32(float2 *v) {
   }
 }
 
-// The same transform with scalar butterflies (kept for comparison).
-template <bool INV>
-__device__ __forceinline__ void dft32_scalar(float2 *v) {
-  float2 a[32];
-#pragma unroll
-  for (int n2 = 0; n2 < 4; ++n2) {
-    float2 t[8];
-#pragma unroll
-    for (int n1 = 0; n1 < 8; ++n1) t[n1] = v[4 * n1 + n2];
-    Dft<8, INV>::run(t, nullptr, 0);
-#pragma unroll
-    for (int k1 = 0; k1 < 8; ++k1) a[n2 * 8 + k1] = t[k1];
-  }
-  // twiddles W32^(n2 k1)
-#define GNC_TW(N2, K1) a[N2 * 8 + K1] = w32<INV, N2 * K1>(a[N2 * 8 + K1])
-  GNC_TW(1, 1); GNC_TW(1, 2); GNC_TW(1, 3); GNC_TW(1, 4); GNC_TW(1, 5); GNC_TW(1, 6); GNC_TW(1, 7);
-  GNC_TW(2, 1); GNC_TW(2, 2); GNC_TW(2, 3); GNC_TW(2, 4); GNC_TW(2, 5); GNC_TW(2, 6); GNC_TW(2, 7);
-  GNC_TW(3, 1); GNC_TW(3, 2); GNC_TW(3, 3); GNC_TW(3, 4); GNC_TW(3, 5); GNC_TW(3, 6); GNC_TW(3, 7);
-#undef GNC_TW
-#pragma unroll
-  for (int k1 = 0; k1 < 8; ++k1) {
-    float2 t[4] = {a[k1], a[8 + k1], a[16 + k1], a[24 + k1]};
-    Dft<4, INV>::run(t, nullptr, 0);
-#pragma unroll
-    for (int k2 = 0; k2 < 4; ++k2) v[k1 + 8 * k2] = t[k2];
-  }
-}
-
 constexpr int kWarpFftSlots = 33 * 32;
 __device__ __forceinline__ int wslot(int k1, int l) { return 33 * k1 + l; }
 
@@ -192,12 +164,9 @@ __device__ __forceinline__ void warp_fft_twiddles(float2 *tw, const float2 *__re
 // kWarpFftSlots shared-memory slots owned by this warp: slot s is
 // tbuf[s * STRIDE] (STRIDE odd).  Contains __syncwarp() only; the slots may be reused by the
 // caller once it has issued another __syncwarp().
-template <bool INV, int STRIDE = 1, bool PACKED = true>
+template <bool INV, int STRIDE = 1>
 __device__ __forceinline__ void warp_fft1024(float2 *v, float2 *tbuf, const float2 *tw, int lane) {
-  if (PACKED)
-    dft32<INV>(v);
-  else
-    dft32_scalar<INV>(v);
+  dft32<INV>(v);
 #pragma unroll
   for (int k1 = 1; k1 < 32; ++k1) {
     float2 w = tw[k1 * 32 + lane];
@@ -210,10 +179,7 @@ __device__ __forceinline__ void warp_fft1024(float2 *v, float2 *tbuf, const floa
   __syncwarp();
 #pragma unroll
   for (int l = 0; l < 32; ++l) v[l] = tbuf[wslot(lane, l) * STRIDE];
-  if (PACKED)
-    dft32<INV>(v);
-  else
-    dft32_scalar<INV>(v);
+  dft32<INV>(v);
 }
 
 }  // namespace gnc

@@ -364,7 +364,6 @@ cudaError_t launch_rfft_rows_p2(const float *proj, float2 *spec, int T, int H, i
   switch (W) {
     case 256: return rfft_rows_p2<256>(proj, spec, T, H, s);
     case 512: return rfft_rows_p2<512>(proj, spec, T, H, s);
-    case 1024: return rfft_rows_p2<1024>(proj, spec, T, H, s);
     case 2048: return rfft_rows_p2<2048>(proj, spec, T, H, s);
     case 4096: return rfft_rows_p2<4096>(proj, spec, T, H, s);
   }
