@@ -6,8 +6,7 @@
 // call: an application that hands this library a fixed device-memory budget
 // and owns every allocation itself, a real-time acquisition loop that must not
 // touch the allocator (an allocation can block on the device or fail under
-// memory pressure at an arbitrary time), or code that records its work into a
-// CUDA graph, where cudaMalloc is not permitted.  For them this file keeps the
+// memory pressure at an arbitrary time).  For them this file keeps the
 // scratch in statically sized device arrays declared at file scope: every GPU
 // that loads the library holds them (about 16.1 MiB) until the process exits,
 // and a call uses them instead of allocating.

@@ -80,8 +80,8 @@ GNC_API int gnc_reconstruct_device(const gnc_config *config, const float *d_sino
 
 /* No counterpart in the reference.  gnc_reconstruct_device without any device
  * allocation, for callers that cannot allocate inside a call: an application
- * that owns a fixed device-memory budget, a real-time loop that must not touch
- * the allocator, or work being recorded into a CUDA graph.  Its scratch lives
+ * that owns a fixed device-memory budget, or a real-time loop that must not
+ * touch the allocator.  Its scratch lives
  * in static device arrays (about 16.1 MiB held by every GPU that loads the
  * library until exit).  Limits: num_defocus * num_angles * num_pixels <=
  * 4194304, num_angles <= 1024, num_pixels <= 4096; larger requests return

@@ -2,8 +2,8 @@
 
 gnc_reconstruct_device_noalloc serves callers that cannot allocate device
 memory inside a call (a fixed device-memory budget owned by the application,
-a real-time loop that must not touch the allocator, work recorded into a CUDA
-graph).  It keeps its scratch in static device arrays instead.  These tests
+a real-time loop that must not touch the allocator).  It keeps its scratch in
+static device arrays instead.  These tests
 call it through the C ABI and check it against gnc_reconstruct_device -- the
 allocating entry point -- within the FP32 parity tolerance, for two calls in a
 row (the second must not see anything the first left in the shared scratch),
