@@ -58,6 +58,24 @@ def voxel_tilts():
     return WL["H"] * WL["Z"] * WL["W"] * WL["T"]
 
 
+def fft_flops():
+    """Nominal flops (5 n log2 n per complex n-point transform) of one step's
+    correction and filter: per tilt the forward row and column transforms (two
+    real rows per complex row, W/2 complex columns); per tilt and slab the
+    inverse column transforms and the ramp filter's four W-point transforms
+    per row pair."""
+    T, H, W = WL["T"], WL["H"], WL["W"]
+    D = WL["D"] if WL["ctf"] else 1
+
+    def f(n):
+        return 5.0 * n * math.log2(n)
+
+    rows = (H + 1) // 2 * 4 * f(W)
+    if not WL["ctf"]:
+        return T * rows
+    return T * ((H + 1) // 2 * f(W) + W // 2 * f(H)) + T * D * (W // 2 * f(H) + rows)
+
+
 def slab_setup():
     import guanaco_gb300 as G
 
@@ -254,6 +272,21 @@ def run_ours(args, rank, world, dist):
     bp_alg = staged_bytes + vol_bytes
     bp_ms = res["f32"][1]
     achieved = bp_alg / (bp_ms * 1e-3) / 1e9
+    # the backprojector's binding resource: shared-memory loads, two 8-byte
+    # pixel pairs per (voxel, row pair, tilt) = 8 bytes per voxel-tilt, against
+    # 128 bytes per clock per SM at the SM clock sampled during the run
+    vt = WL["T"] * WL["H"] * WL["Z"] * WL["W"]
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    sm_mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz")
+    smem_peak = sms * 128 * sm_mhz * 1e6 / 1e9 if sm_mhz else None
+    smem_achieved = 8 * vt / (bp_ms * 1e-3) / 1e9
+    # correction + filter stage (everything before the backprojection): HBM
+    # bytes of the fused stage (raw projections in, staged rows out; the
+    # flipped spectra pass through L2 tilt by tilt) and its FFT work at the
+    # nominal 5 n log2 n flops per complex n-point transform
+    stage_ms = total32 / args.steps - bp_ms
+    stage_bytes = WL["T"] * WL["H"] * WL["W"] * 4 + staged_bytes
+    stage_flops = fft_flops()
     line = {
         "metric": METRIC,
         "value": round(value32, 2),
@@ -301,6 +334,23 @@ def run_ours(args, rank, world, dist):
             "traffic": BP_TRAFFIC_BYTES["f32"] if args.case == "3dctf" else None,
             "algorithmic_bytes": bp_alg,
             "kernel_ms": round(bp_ms, 4),
+            "binding": {
+                "resource": "shared-memory loads (8 B per voxel-tilt)",
+                "achieved": round(smem_achieved, 1),
+                "peak": round(smem_peak, 1) if smem_peak else None,
+                "unit": "GB/s",
+                "frac": round(smem_achieved / smem_peak, 4) if smem_peak else None,
+                "peak_source": f"{sms} SMs x 128 B/clk x {sm_mhz} MHz (sampled SM clock)",
+            },
+            "correction_filter_stage": {
+                "ms": round(stage_ms, 4),
+                "algorithmic_bytes": stage_bytes,
+                "achieved": round(stage_bytes / (stage_ms * 1e-3) / 1e9, 1),
+                "unit": "GB/s",
+                "frac": round(stage_bytes / (stage_ms * 1e-3) / 1e9 / hbm_peak, 4),
+                "fft_tflops_nominal": round(stage_flops / (stage_ms * 1e-3) / 1e12, 2),
+                "bound": "FP32 and shared-memory instruction issue of the register FFTs",
+            },
         },
         "clocks": clk,
         # kernels of this library launched in the timed region of `value`
