@@ -20,8 +20,7 @@
 //    contents: calls that may overlap on the GPU (different streams, or host
 //    threads racing) race on them and must be serialised by the caller;
 //  * the first call on a device looks up the arrays' device addresses
-//    (cudaGetSymbolAddress with that device current), so make the first call
-//    on each device before any stream capture.
+//    (cudaGetSymbolAddress with that device current) and keeps them.
 #include <math.h>
 
 #include <mutex>

@@ -87,8 +87,7 @@ GNC_API int gnc_reconstruct_device(const gnc_config *config, const float *d_sino
  * 4194304, num_angles <= 1024, num_pixels <= 4096; larger requests return
  * GNC_ERR_INVALID_ARGUMENT.  All calls on a device share the scratch, so calls
  * that overlap on the GPU race; serialise them.  The first call on a device
- * looks the scratch up (cudaGetSymbolAddress) and should come before any
- * stream capture. */
+ * looks up the scratch's device addresses (cudaGetSymbolAddress). */
 GNC_API int gnc_reconstruct_device_noalloc(const gnc_config *config, const float *d_sinogram,
                                            float *d_reconstruction, void *stream);
 
