@@ -219,10 +219,17 @@ void capture(gnc_server *S, Cached *c) {
 
 // Without the lock: everything one request puts on its slot's stream; with
 // may_capture (the builder), a plan without a graph captures one afterwards.
+// On failure, whatever was already queued for the request has finished when
+// this returns, so the caller may hand the slot, the plan and the caller's
+// host buffers back.
 int enqueue(gnc_server *S, Slot *sl, Request *r, Cached *c, bool may_capture) {
   cudaStream_t s = sl->s;
+  auto drained = [s](int status) {
+    cudaStreamSynchronize(s);
+    return status;
+  };
   int st = gnc::plan_set_request(c->plan, &r->desc, c->h_params, s);
-  if (st != GNC_OK) return st;
+  if (st != GNC_OK) return drained(st);
   cudaError_t e = cudaMemcpyAsync(c->d_in, r->h_in, r->in_bytes, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) {
     if (c->exec) {
@@ -230,7 +237,7 @@ int enqueue(gnc_server *S, Slot *sl, Request *r, Cached *c, bool may_capture) {
       r->graph = 1;
     } else {
       st = gnc_fbp_execute(c->plan, c->d_in, c->d_out, s);
-      if (st != GNC_OK) return st;
+      if (st != GNC_OK) return drained(st);
     }
   }
   if (e == cudaSuccess)
@@ -241,7 +248,7 @@ int enqueue(gnc_server *S, Slot *sl, Request *r, Cached *c, bool may_capture) {
   if (e == cudaSuccess) e = cudaLaunchHostFunc(s, on_done, sl);
   if (e != cudaSuccess) {
     gnc::set_error(std::string("gnc_server: ") + cudaGetErrorString(e));
-    return GNC_ERR_CUDA;
+    return drained(GNC_ERR_CUDA);
   }
   if (may_capture && !c->exec) capture(S, c);
   return GNC_OK;
