@@ -7,6 +7,13 @@ blob phantoms (the reference publishes no dataset):
   512 x 512 projections at 1.35 A/px, 300 kV, Cs 2.7 mm, defocus 20000 A,
   volume 512 x 256 x 512 (the oracle checks a band of 48 rows).
 
+* 3D CTF: 61 tilts over +-60 deg, 1024 x 1024 projections at 1.0 A/px, 300 kV,
+  Cs 2.7 mm, defocus 30000 A, ten defocus slabs, volume 1024 x 1024 x 300 (the
+  oracle checks a band of 8 rows);
+* large 3D CTF: 61 tilts of 4096 x 4096 at 0.8 A/px, defocus 40000 A, twenty
+  slabs, volume 4096 x 4096 x 512 (8.6e9 voxels, 1.0e10 staged pixels: past
+  2^32 elements), checked by properties the oracle cannot reach at this size.
+
 FP32 against the reference CPU path (float oracle) and the FP64 oracle within
 1e-4 relative L2; FP16 staging against the FP64 oracle within 1e-3.
 """
@@ -87,3 +94,102 @@ def test_single_defocus_ctf_512(G, oracle, staging):
         assert rel_l2(vol[sl], ref64) < FP32_TOL
     else:
         assert rel_l2(vol[sl], ref64) < FP16_TOL
+
+
+@pytest.fixture(scope="module")
+def series_3dctf(G, oracle):
+    """The 3D-CTF series and the two oracles on rows 508..515."""
+    T, n, Z, ps, df, D = 61, 1024, 300, 1.0, 30000.0, 10
+    ang, proj = _series(G, T, n, Z, 2000, seed=2, defocus=df, pixel_size=ps)
+    c = G.get_centre((T, n, n), None, False)
+    mn, mx, step, nd = G.get_defocus_steps(df, D, None, n, c, ps)
+    assert nd == D
+    ctf = oracle.ctf_stack(n, n, ps, 300, mn, nd, step, 2.7)
+    rows = (n // 2 - 4, n // 2 + 4)
+    args = (proj, ang, c, ps, ctf, float(mn - df), float(mx - df))
+    ref32 = oracle.fbp_ctf(*args, Z=Z, rows=rows, precision="f32")[slice(*rows)]
+    ref64 = oracle.fbp_ctf(*args, Z=Z, rows=rows, precision="f64")[slice(*rows)]
+    desc = dict(grid_height=Z, centre=c, pixel_size=ps, correct=True, num_defocus=nd,
+                slab_defocus=G.api.slab_defoci(mn, nd, step), min_defocus=float(mn - df),
+                max_defocus=float(mx - df), energy=300.0, spherical_aberration=2.7)
+    return ang, proj, desc, rows, ref32, ref64
+
+
+@pytest.mark.parametrize("staging", ["f32", "f16"])
+def test_3dctf_ndf10_1024(G, series_3dctf, staging):
+    ang, proj, desc, rows, ref32, ref64 = series_3dctf
+    T, n = proj.shape[0], proj.shape[2]
+    plan = G.FbpPlan(T, n, n, ang, staging=staging, **desc)
+    vol = plan.execute_host(proj)
+    plan.close()
+    got = vol[slice(*rows)]
+    if staging == "f32":
+        assert rel_l2(got, ref32) < FP32_TOL
+        assert rel_l2(got, ref64) < FP32_TOL
+    else:
+        assert rel_l2(got, ref64) < FP16_TOL
+
+
+def test_large_plain_fbp_rows_match_a_band_plan(G):
+    """Plain FBP at the large configuration's size (4096 x 4096 x 512 volume):
+    rows are independent, so the last and first rows of the whole volume must
+    equal, bit for bit, a plan over just those rows; the last rows' volume
+    offsets pass 2^32 elements."""
+    import torch
+
+    T, n, Z, band = 61, 4096, 512, 8
+    ang = np.deg2rad(np.linspace(-60, 60, T)).astype(np.float32)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(7)
+    proj = torch.randn((T, n, n), device="cuda", generator=g)
+    full = G.FbpPlan(T, n, n, ang, grid_height=Z, centre=n / 2, correct=False)
+    vol = torch.empty(full.volume_shape, dtype=torch.float32, device="cuda")
+    full.execute(proj, vol)
+    torch.cuda.synchronize()
+    full.close()
+    for y0 in (0, n - band):
+        sub = G.FbpPlan(T, band, n, ang, grid_height=Z, centre=n / 2, correct=False)
+        part = torch.empty(sub.volume_shape, dtype=torch.float32, device="cuda")
+        sub.execute(proj[:, y0:y0 + band].contiguous(), part)
+        torch.cuda.synchronize()
+        sub.close()
+        assert torch.equal(vol[y0:y0 + band], part), y0
+        assert float(part.abs().max()) > 0
+    del vol
+    torch.cuda.empty_cache()
+
+
+def test_large_3dctf_host_path_equals_device_path(G):
+    """The large 3D-CTF configuration end to end: the host-buffer path (input in
+    tilt groups, volume out in row slabs, 34 GB to host memory) gives the
+    device path's volume bit for bit on bands at the start, middle and end."""
+    import torch
+
+    from guanaco_gb300 import serve
+
+    T, n, Z, ps, df, D = 61, 4096, 512, 0.8, 40000.0, 20
+    ang = np.deg2rad(np.linspace(-60, 60, T)).astype(np.float32)
+    c = G.get_centre((T, n, n), None, False)
+    mn, mx, step, nd = G.get_defocus_steps(df, D, None, n, c, ps)
+    assert nd == D
+    g = torch.Generator(device="cuda")
+    g.manual_seed(11)
+    proj = torch.randn((T, n, n), device="cuda", generator=g)
+    plan = G.FbpPlan(T, n, n, ang, grid_height=Z, centre=c, pixel_size=ps, correct=True,
+                     num_defocus=nd, slab_defocus=G.api.slab_defoci(mn, nd, step),
+                     min_defocus=float(mn - df), max_defocus=float(mx - df), energy=300.0,
+                     spherical_aberration=2.7)
+    want = torch.empty(plan.volume_shape, dtype=torch.float32, device="cuda")
+    plan.execute(proj, want)
+    torch.cuda.synchronize()
+    h_in = serve.pinned_empty(tuple(proj.shape))
+    h_in[...] = proj.cpu().numpy()
+    h_out = serve.pinned_empty(plan.volume_shape)
+    plan.execute_host(h_in, h_out)
+    plan.close()
+    for y0 in (0, n // 2 - 4, n - 8):
+        a = want[y0:y0 + 8].cpu().numpy()
+        np.testing.assert_array_equal(h_out[y0:y0 + 8], a)
+        assert float(np.abs(a).max()) > 0
+    del want
+    torch.cuda.empty_cache()
