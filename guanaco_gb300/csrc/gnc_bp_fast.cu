@@ -117,6 +117,27 @@ __device__ __forceinline__ void mbar_wait(u64 *bar, unsigned parity, int *err) {
   if (err) atomicOr(err, 1);
 }
 
+// FP16 form: acc (two f32 lanes) += val * f for the two halves of val and f;
+// the FP16 product is exact in FP32, so each lane rounds once, as an FP32 FMA
+// of the converted values would
+__device__ __forceinline__ void acc_f16(u64 &acc, unsigned val, unsigned f) {
+  asm("{ .reg .f32 lo, hi; .reg .b16 vl, vh, fl, fh;\n\t"
+      "mov.b64 {lo, hi}, %0;\n\t"
+      "mov.b32 {vl, vh}, %1;\n\t"
+      "mov.b32 {fl, fh}, %2;\n\t"
+      "fma.rn.f32.f16 lo, vl, fl, lo;\n\t"
+      "fma.rn.f32.f16 hi, vh, fh, hi;\n\t"
+      "mov.b64 %0, {lo, hi}; }"
+      : "+l"(acc)
+      : "r"(val), "r"(f));
+}
+
+// 2^d as a float (d clamped to the normal exponent range)
+__device__ __forceinline__ float exp2_int(int d) {
+  d = max(-126, min(127, d));
+  return __int_as_float((127 + d) << 23);
+}
+
 // ceil(sqrt(v)) for a non-negative integer, at compile time
 constexpr int isqrt_ceil(int v) {
   int r = 0;
@@ -176,12 +197,17 @@ k_bp_fast(BpArgs a) {
   constexpr int TCH = P::TCH;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ TiltParams s_tp[TCH];
-  // FP16: per (tilt, row pair) the BP scale times 2^-e of the row pair's
-  // reference exponent (the smallest over the tile's slabs), and per (tilt,
-  // row pair, slab) the half2 power of two 2^(e_ref - e) that brings that
-  // slab's staged values to the reference (1 for most slots)
-  __shared__ float2 s_rs[F16 ? TCH * RP : 1];
+  // FP16: a row's staged values carry 2^e (e per row, slab and tilt).  Per
+  // (tilt, row pair, slab) the half2 power of two 2^(e_ref - e) brings a slab's
+  // values to the pair's reference exponent e_ref of that tilt (the smallest
+  // over the tile's slabs; 1 for most slots), and per (tilt, row pair) the
+  // half2 power of two 2^(E - e_ref) brings the tilt to E, the smallest e_ref
+  // over the chunk's tilts (two lanes: rows a and b).  The accumulators hold
+  // sums in units of 2^-E: they are rescaled when a chunk changes E, and times
+  // the backprojection scale and 2^-E when stored.
+  __shared__ unsigned s_fs[F16 ? TCH * RP : 1];
   __shared__ unsigned s_fac[F16 ? TCH * RP * KMAX : 1];
+  __shared__ int s_E[2][F16 ? 2 * RP : 1];  // E of this chunk and of the previous one
   __shared__ __align__(8) u64 s_bar[2];
 
   const int tid = threadIdx.x;
@@ -259,6 +285,8 @@ k_bp_fast(BpArgs a) {
   for (int tbase = 0; tbase < a.T; tbase += TCH) {
     const int nch = min(TCH, a.T - tbase);
     __syncthreads();  // the previous chunk's parameters and buffers are no longer read
+    const int ci = tbase / TCH;  // chunk index
+    if (F16 && tid < 2 * RP) s_E[ci & 1][tid] = 127;
     for (int tl = tid; tl < nch; tl += P::NT) {
       const int t = tbase + tl;
       const TiltGeom g = a.geom[t];
@@ -310,14 +338,36 @@ k_bp_fast(BpArgs a) {
             rb = min(rb, eb[sl]);
           }
         }
-        if (ra == 127) ra = rb = 0;  // no staged rows for this pair
-        const float sc = a.geom[tbase + tl].scale;
-        s_rs[e] = make_float2(sc * __int_as_float((127 - ra) << 23),
-                              sc * __int_as_float((127 - rb) << 23));
+        if (ra == 127) {
+          ra = rb = 0;  // no staged rows for this pair (nothing stored either)
+        } else {
+          atomicMin(&s_E[ci & 1][2 * r], ra);
+          atomicMin(&s_E[ci & 1][2 * r + 1], rb);
+        }
+        s_fs[e] = (unsigned)(ra + 128) | ((unsigned)(rb + 128) << 16);  // until E is known
 #pragma unroll
         for (int sl = 0; sl < KMAX; ++sl)
           s_fac[e * KMAX + sl] = half_pow2_neg(ea[sl] == 127 ? 0 : ea[sl] - ra) |
                                  (half_pow2_neg(eb[sl] == 127 ? 0 : eb[sl] - rb) << 16);
+      }
+      __syncthreads();
+      for (int e = tid; e < nch * RP; e += P::NT) {
+        const int r = e % RP;
+        const int ra = (int)(s_fs[e] & 0xffffu) - 128, rb = (int)(s_fs[e] >> 16) - 128;
+        const int Ea = min(s_E[ci & 1][2 * r], ra), Eb = min(s_E[ci & 1][2 * r + 1], rb);
+        s_fs[e] = half_pow2_neg(ra - Ea) | (half_pow2_neg(rb - Eb) << 16);
+      }
+      if (ci > 0) {  // accumulators from units of the previous chunk's 2^-E to this one's
+#pragma unroll
+        for (int rr = 0; rr < RP; ++rr) {
+          const int da = s_E[ci & 1][2 * rr] - s_E[(ci - 1) & 1][2 * rr];
+          const int db = s_E[ci & 1][2 * rr + 1] - s_E[(ci - 1) & 1][2 * rr + 1];
+          const u64 f = f2_pack(exp2_int(da), exp2_int(db));
+#pragma unroll
+          for (int i = 0; i < A; ++i)
+#pragma unroll
+            for (int j = 0; j < B; ++j) acc[i][j][rr] = f2_fma(acc[i][j][rr], f, 0ull);
+        }
       }
       __syncthreads();
     }
@@ -372,14 +422,11 @@ k_bp_fast(BpArgs a) {
         // the magic-number bias of the float bits folds into the same
         // constant (unsigned arithmetic wraps modulo 2^32 and cancels exactly)
         const unsigned bias = (unsigned)(-tp.p_s * P::PB) - (unsigned)kMagicBits * P::PB;
-        u64 rs[RP];
+        u64 rs[RP];        // FP32: the tilt's scale, both rows
+        unsigned fs[RP];   // FP16: 2^(E - e_ref), half2
         if (F16) {
-          const float2 *trs = s_rs + (size_t)(tg + gi) * RP;
 #pragma unroll
-          for (int rr = 0; rr < RP; ++rr) {
-            const float2 f = trs[rr];
-            rs[rr] = f2_pack(f.x, f.y);
-          }
+          for (int rr = 0; rr < RP; ++rr) fs[rr] = s_fs[(tg + gi) * RP + rr];
         } else {
 #pragma unroll
           for (int rr = 0; rr < RP; ++rr) rs[rr] = f2_pack(tp.scale, tp.scale);
@@ -430,8 +477,8 @@ k_bp_fast(BpArgs a) {
                   const unsigned char *p = p0 + rr * KMAX * P::SLOT_BYTES;
                   const uint2 rec = *(const uint2 *)p;  // (v_a, v_b), (dv_a, dv_b)
                   const __half2 v0 = *(const __half2 *)&rec.x, dv = *(const __half2 *)&rec.y;
-                  const float2 val = __half22float2(__hfma2(t2, dv, v0));
-                  acc[i][j][rr] = f2_fma(f2_pack(val.x, val.y), rs[rr], acc[i][j][rr]);
+                  const __half2 val = __hfma2(t2, dv, v0);
+                  acc_f16(acc[i][j][rr], *(const unsigned *)&val, fs[rr]);
                 }
               } else {
                 const u64 tt = f2_pack(t, t);
@@ -455,8 +502,15 @@ k_bp_fast(BpArgs a) {
     }
   }
   // ---- store
+  // FP16: from units of 2^-E (the last chunk's E) to the volume, times the
+  // backprojection scale pi / (2 T) |ray| / |d| of the first tilt (it differs
+  // between tilts only in the last bits of the float cos^2 + sin^2)
+  const int cl = ((a.T - 1) / TCH) & 1;
+  const float sc = F16 ? a.geom[0].scale : 1.f;
 #pragma unroll
   for (int rr = 0; rr < RP; ++rr) {
+    const float fa = F16 ? sc * exp2_int(-s_E[cl][2 * rr]) : 1.f;
+    const float fb = F16 ? sc * exp2_int(-s_E[cl][2 * rr + 1]) : 1.f;
     const int ya = 2 * (y2_0 + rr), yb = ya + 1;
 #pragma unroll
     for (int j = 0; j < B; ++j) {
@@ -466,7 +520,8 @@ k_bp_fast(BpArgs a) {
       for (int i = 0; i < A; ++i) {
         const int x = x0 + wx * 4 * A + 4 * i + lx;
         if (x >= a.X) continue;
-        const float2 v = f2_unpack(acc[i][j][rr]);
+        float2 v = f2_unpack(acc[i][j][rr]);
+        if (F16) v = make_float2(v.x * fa, v.y * fb);
         if (ya < a.Y) a.vol[((size_t)ya * a.Z + z) * a.X + x] = v.x;
         if (yb < a.Y) a.vol[((size_t)yb * a.Z + z) * a.X + x] = v.y;
       }

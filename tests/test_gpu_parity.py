@@ -269,6 +269,26 @@ def test_pipeline_vs_oracles(torch, oracle, staging, shape):
         assert rel_l2(vol, ref64) < FP16_TOL
 
 
+# More tilts than the backprojector holds parameters for at once (128): it
+# runs them in chunks.  Tilts of very different magnitude per chunk change the
+# FP16 form's common exponent from chunk to chunk, so its accumulators are
+# rescaled at each chunk boundary.
+@pytest.mark.parametrize("staging", ["f32", "f16"])
+def test_tilt_chunks_of_different_magnitude(torch, oracle, staging):
+    T, H, W, Z, D = 300, 6, 48, 32, 3
+    plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=T, H=H, W=W, Z=Z, D=D, staging=staging)
+    proj[128:256] *= 40.0
+    proj[256:] *= 1.0 / 30.0
+    vol = plan.execute_host(proj)
+    ref32 = _oracle_volume(oracle, proj, ang, c, ctf, mn, mx, Z, "f32")
+    ref64 = _oracle_volume(oracle, proj, ang, c, ctf, mn, mx, Z, "f64")
+    if staging == "f32":
+        assert rel_l2(vol, ref32) < FP32_TOL
+        assert rel_l2(vol, ref64) < FP32_TOL
+    else:
+        assert rel_l2(vol, ref64) < FP16_TOL
+
+
 # The host-buffer entry point overlaps its copies with the kernels (tilt groups
 # in, row slabs out; with CTF correction it filters row slab by row slab); it
 # must give exactly the device entry point's volume.  Shapes: power-of-two and
