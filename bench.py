@@ -222,11 +222,11 @@ def run_ours(args, rank, world, dist):
             torch.cuda.empty_cache()
     # end to end through the public host-buffer entry point: pinned input in,
     # volume out, every step
-    h_in = torch.empty(proj.shape, dtype=torch.float32, pin_memory=True)
-    h_in.copy_(proj)
-    h_in_np = h_in.numpy()
-    h_out = torch.empty((WL["H"], WL["Z"], WL["W"]), dtype=torch.float32, pin_memory=True)
-    h_out_np = h_out.numpy()
+    from guanaco_gb300 import serve
+
+    h_in_np = serve.pinned_empty(tuple(proj.shape))
+    h_in_np[...] = proj.cpu().numpy()
+    h_out_np = serve.pinned_empty((WL["H"], WL["Z"], WL["W"]))
     plans["f32"].execute_host(h_in_np, h_out_np, stream)
     barrier()
     t0 = time.perf_counter()

@@ -132,6 +132,8 @@ SIGNATURES = {
     "gnc_fbp_workspace_bytes": (c_size, [c_void]),
     "gnc_fbp_execute": (c_int, [c_void, c_void, c_void, c_void]),
     "gnc_fbp_execute_host": (c_int, [c_void, c_void, c_void, c_void]),
+    "gnc_host_alloc": (c_int, [c_size, ctypes.POINTER(c_void)]),
+    "gnc_host_free": (c_int, [c_void]),
     "gnc_fbp_correct": (c_int, [c_void, c_void, c_void, c_void]),
     "gnc_fbp_stage": (c_int, [c_void, c_void, c_void]),
     "gnc_fbp_backproject": (c_int, [c_void, c_void, c_int, c_void]),

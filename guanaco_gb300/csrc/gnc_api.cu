@@ -729,6 +729,18 @@ static int execute_host_pipelined(gnc_fbp_plan *p, const float *h_input, float *
   return GNC_OK;
 }
 
+int gnc_host_alloc(size_t bytes, void **ptr) {
+  GNC_REQUIRE(ptr != nullptr && bytes > 0);
+  *ptr = nullptr;
+  GNC_CUDA(cudaHostAlloc(ptr, bytes, cudaHostAllocDefault));
+  return GNC_OK;
+}
+
+int gnc_host_free(void *ptr) {
+  if (ptr) GNC_CUDA(cudaFreeHost(ptr));
+  return GNC_OK;
+}
+
 int gnc_fbp_execute_host(gnc_fbp_plan *p, const float *h_input, float *h_volume, void *stream) {
   GNC_REQUIRE(p != nullptr && h_input != nullptr && h_volume != nullptr);
   cudaStream_t s = (cudaStream_t)stream;

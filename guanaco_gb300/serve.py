@@ -21,12 +21,29 @@ from . import _lib
 from .fbp import FbpDesc
 
 
-def pinned_empty(shape, dtype=np.float32):
-    """A page-locked host array (allocated through torch's CUDA host allocator)."""
-    import torch
+class _PinnedBlock:
+    """Exactly the array's bytes of page-locked host memory (gnc_host_alloc; a
+    caching host allocator would round a 34 GB volume up to 64 GB of locked
+    pages), freed when the last array over it is gone."""
 
-    t = torch.empty(tuple(shape), dtype=getattr(torch, np.dtype(dtype).name), pin_memory=True)
-    return t.numpy()
+    def __init__(self, shape, dtype):
+        self._lib = _lib.load()
+        nbytes = max(1, int(np.prod(shape, dtype=np.int64)) * dtype.itemsize)
+        ptr = ctypes.c_void_p()
+        _lib.check(self._lib.gnc_host_alloc(nbytes, ctypes.byref(ptr)))
+        self._ptr = ptr.value
+        self.__array_interface__ = dict(shape=tuple(int(n) for n in shape), typestr=dtype.str,
+                                        data=(self._ptr, False), version=3)
+
+    def __del__(self):
+        if getattr(self, "_ptr", None):
+            self._lib.gnc_host_free(self._ptr)
+            self._ptr = None
+
+
+def pinned_empty(shape, dtype=np.float32):
+    """A page-locked host array of exactly its own size."""
+    return np.asarray(_PinnedBlock(tuple(shape), np.dtype(dtype)))
 
 
 class Server:

@@ -214,6 +214,12 @@ GNC_API int gnc_fbp_execute(gnc_fbp_plan *plan, const float *d_input, float *d_v
  * copies. */
 GNC_API int gnc_fbp_execute_host(gnc_fbp_plan *plan, const float *h_input, float *h_volume,
                                  void *stream);
+/* No counterpart in the reference.  Page-locked host memory of exactly `bytes`
+ * (cudaHostAlloc) for the host buffers of gnc_fbp_execute_host and of the
+ * request server: copies from and to it run at the host link's full rate.
+ * Release with gnc_host_free. */
+GNC_API int gnc_host_alloc(size_t bytes, void **ptr);
+GNC_API int gnc_host_free(void *ptr);
 /* Correction only: raw (T, H, W) -> corrected stack (T, D, H, W), the output
  * of correct_projections (correct.py:276-303), device pointers. */
 GNC_API int gnc_fbp_correct(gnc_fbp_plan *plan, const float *d_proj, float *d_corrected,
