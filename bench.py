@@ -166,6 +166,24 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# ------------------------------------------------------------- N replicas
+def reduce_max_over_ranks(values, dist, device):
+    """Each timing's maximum over the ranks: the slowest replica sets the job's
+    time.  ``dist`` is torch.distributed (or None for one rank)."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
+def job_throughput(units_per_step, steps, world, ms):
+    """Whole-job Gvoxel·tilt/s: every replica's units over the slowest time."""
+    return units_per_step * steps * world / (ms * 1e-3) / 1e9
+
+
 # --------------------------------------------------------------- our arm
 def run_ours(args, rank, world, dist):
     import torch
@@ -236,20 +254,11 @@ def run_ours(args, rank, world, dist):
     e2e_ms = (time.perf_counter() - t0) * 1e3
     clk = clocks.stop()
 
-    def reduce_max(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-
-    total32 = reduce_max(res["f32"][0])
-    total16 = reduce_max(res["f16"][0])
-    e2e_ms = reduce_max(e2e_ms)
-    units = voxel_tilts() * args.steps * world
-    value32 = units / (total32 * 1e-3) / 1e9
-    value16 = units / (total16 * 1e-3) / 1e9
-    e2e_value = units / (e2e_ms * 1e-3) / 1e9
+    total32, total16, e2e_ms = reduce_max_over_ranks([res["f32"][0], res["f16"][0], e2e_ms],
+                                                     dist, dev)
+    value32 = job_throughput(voxel_tilts(), args.steps, world, total32)
+    value16 = job_throughput(voxel_tilts(), args.steps, world, total16)
+    e2e_value = job_throughput(voxel_tilts(), args.steps, world, e2e_ms)
 
     serving = run_serving(dev) if not args.no_serve else None
     parity = cpu = None
