@@ -177,8 +177,11 @@ struct FastBp {
   // pixels a bulk copy may write into one slot (window + alignment, rounded)
   static constexpr int NPX_MAX = ((WIN + 2 * ALIGN) / ALIGN) * ALIGN;
   // every slot ends in ALIGN zero pixels that copies never touch: voxels off
-  // the detector read their (v0, v1) pair there
-  static constexpr int SLOT = NPX_MAX + ALIGN;
+  // the detector read their (v0, v1) pair there.  The slot length is 8 modulo
+  // the 16 eight-byte bank pairs: the lanes of a half warp that read two slabs'
+  // slots (pixel spans of at most 8) then fall half a bank cycle apart.
+  static constexpr int SLOT0 = NPX_MAX + ALIGN;
+  static constexpr int SLOT = SLOT0 + (24 - SLOT0 % 16) % 16;
   static constexpr int SLOT_BYTES = SLOT * PB;
   static constexpr int ROWS = G * RP * KMAX;      // slots per buffer
   static constexpr size_t BUF = (size_t)ROWS * SLOT_BYTES;
