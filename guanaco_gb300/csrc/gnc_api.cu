@@ -141,6 +141,15 @@ constexpr int kIoGroups = 32, kIoSlabs = 10, kIoEvents = kIoGroups + kIoSlabs + 
 // Largest phase-flipped spectrum stack (T, D, H, W/2) the host-buffer path
 // keeps whole so that it can filter and backproject row slab by row slab.
 constexpr size_t kSlabMajorMaxBytes = (size_t)8 << 30;
+// Tilts whose phase-flipped spectra one flip launch produces and one row-stage
+// launch consumes (two such chunks in flight): enough tilts for 48 MB, at
+// least 4 while that stays within 192 MB (1024^2 x ten slabs: 4 tilts of
+// 42 MB; larger launches fill the GPU's last wave better than L2-sized ones
+// save in traffic), at least 1.
+static size_t flip_chunk(size_t T, size_t per_tilt) {
+  const size_t by_l2 = ((size_t)48 << 20) / per_tilt, cap = ((size_t)192 << 20) / per_tilt;
+  return std::max<size_t>(1, std::min<size_t>(T, std::min(cap, std::max<size_t>(4, by_l2))));
+}
 
 // Per-request parameter block of a plan: the same byte layout on the host and
 // on the device, so one copy moves all of it.
@@ -345,7 +354,7 @@ size_t plan_bytes(const gnc_fbp_desc *d) {
   size_t b = param_layout((int)T, (int)H, (int)D).bytes + sizeof(int);
   if (ctf) {
     const size_t per_tilt = D * H * half * sizeof(float2);
-    const size_t chunk = std::max<size_t>(1, std::min<size_t>(T, (48ull << 20) / per_tilt));
+    const size_t chunk = flip_chunk(T, per_tilt);
     b += T * H * half * sizeof(float2) + 2 * chunk * D * H * half * sizeof(float2) +
          sign_table_bytes((int)D, (int)H, (int)W);
   }
@@ -444,7 +453,7 @@ int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
   }
   if (ctf) {
     size_t per_tilt = (size_t)p->D * p->H * half * sizeof(float2);
-    p->chunk = (int)std::max<size_t>(1, std::min<size_t>(p->T, (48ull << 20) / per_tilt));
+    p->chunk = (int)flip_chunk(p->T, per_tilt);
     if (e == cudaSuccess) e = dalloc(p, &p->spec, (size_t)p->T * p->H * half);
     if (e == cudaSuccess) e = dalloc(p, &p->gbuf, 2 * (size_t)p->chunk * p->D * p->H * half);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->s_flip, cudaStreamNonBlocking);
