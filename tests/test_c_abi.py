@@ -145,3 +145,68 @@ def test_unsupported_sizes_reported(lib):
     with pytest.raises(_lib.GncError) as ei:  # 2 * 4099 has a prime factor > 16
         FbpPlan(3, 8, 4099, np.zeros(3, np.float32), correct=False)
     assert ei.value.status == _lib.GNC_ERR_UNSUPPORTED
+
+
+# Each argument check of the reference's pybind entry points
+# (src/guanaco/detail/ext/reconstruct.h:46-58, correct.h:38-54) raises the same
+# "ASSERT (condition) failed" RuntimeError here, before any device work.
+_F = np.float32
+_RECON_CASES = [
+    ((np.zeros(8, _F), np.zeros((8, 8), _F), np.zeros(3, _F)),
+     "sinogram.ndim() == 2 || sinogram.ndim() == 3"),
+    ((np.zeros((3, 8), _F), np.zeros(64, _F), np.zeros(3, _F)), "reconstruction.ndim() == 2"),
+    ((np.zeros((3, 8), _F), np.zeros((8, 8), _F), np.zeros((3, 1), _F)), "angles.ndim() == 1"),
+    ((np.zeros((3, 8), _F), np.zeros((8, 8), _F), np.zeros(4, _F)),
+     "sinogram.shape()[0] == angles.size()"),
+    ((np.zeros((3, 8), _F), np.zeros((7, 8), _F), np.zeros(3, _F)),
+     "sinogram.shape()[1] == reconstruction.shape()[0]"),
+    ((np.zeros((3, 8), _F), np.zeros((8, 7), _F), np.zeros(3, _F)),
+     "sinogram.shape()[1] == reconstruction.shape()[1]"),
+    ((np.zeros((2, 3, 8), _F), np.zeros((8, 8), _F), np.zeros(4, _F)),
+     "sinogram.shape()[1] == angles.size()"),
+    ((np.zeros((2, 3, 8), _F), np.zeros((7, 8), _F), np.zeros(3, _F)),
+     "sinogram.shape()[2] == reconstruction.shape()[0]"),
+    ((np.zeros((2, 3, 8), _F), np.zeros((8, 7), _F), np.zeros(3, _F)),
+     "sinogram.shape()[2] == reconstruction.shape()[1]"),
+]
+
+
+@pytest.mark.parametrize("args,cond", _RECON_CASES)
+def test_recon_argument_checks(lib, args, cond):
+    from guanaco_gb300 import detail
+
+    sino, rec, ang = args
+    with pytest.raises(RuntimeError) as e:
+        detail.recon(sino, rec, ang, 4.0, device="gpu")
+    assert str(e.value) == f"ASSERT ({cond}) failed"
+
+
+_C = np.complex64
+_CORR_CASES = [
+    ((np.zeros(6, _F), np.zeros((4, 6), _C), np.zeros((4, 6), _F)), "image.ndim() == 2"),
+    ((np.zeros((4, 6), _F), np.zeros(6, _C), np.zeros((4, 6), _F)),
+     "ctf.ndim() == 2 || ctf.ndim() == 3"),
+    ((np.zeros((4, 6), _F), np.zeros((2, 4, 6), _C), np.zeros((4, 6), _F)),
+     "rec.ndim() == image.ndim() + (ctf.ndim() - 2)"),
+    ((np.zeros((4, 6), _F), np.zeros((0, 4, 6), _C), np.zeros((0, 4, 6), _F)), "num_ctf > 0"),
+    ((np.zeros((0, 6), _F), np.zeros((0, 6), _C), np.zeros((0, 6), _F)), "ysize > 0"),
+    ((np.zeros((4, 0), _F), np.zeros((4, 0), _C), np.zeros((4, 0), _F)), "xsize > 0"),
+    ((np.zeros((4, 6), _F), np.zeros((5, 6), _C), np.zeros((4, 6), _F)),
+     "ctf.shape()[ctf.ndim() - 2] == ysize"),
+    ((np.zeros((4, 6), _F), np.zeros((4, 5), _C), np.zeros((4, 6), _F)),
+     "ctf.shape()[ctf.ndim() - 1] == xsize"),
+    ((np.zeros((4, 6), _F), np.zeros((4, 6), _C), np.zeros((5, 6), _F)),
+     "rec.shape()[rec.ndim() - 2] == ysize"),
+    ((np.zeros((4, 6), _F), np.zeros((4, 6), _C), np.zeros((4, 5), _F)),
+     "rec.shape()[rec.ndim() - 1] == xsize"),
+]
+
+
+@pytest.mark.parametrize("args,cond", _CORR_CASES)
+def test_corr_argument_checks(lib, args, cond):
+    from guanaco_gb300 import detail
+
+    image, ctf, rec = args
+    with pytest.raises(RuntimeError) as e:
+        detail.corr(image, ctf, rec, device="gpu")
+    assert str(e.value) == f"ASSERT ({cond}) failed"
