@@ -210,3 +210,17 @@ def test_corr_argument_checks(lib, args, cond):
     with pytest.raises(RuntimeError) as e:
         detail.corr(image, ctf, rec, device="gpu")
     assert str(e.value) == f"ASSERT ({cond}) failed"
+
+
+def test_host_alloc_argument_checks(lib):
+    """gnc_host_alloc rejects a null result pointer and a zero size before any
+    CUDA call; gnc_host_free of null is a no-op."""
+    import ctypes
+
+    from guanaco_gb300 import _lib
+
+    ptr = ctypes.c_void_p(1234)
+    assert lib.gnc_host_alloc(0, ctypes.byref(ptr)) == _lib.GNC_ERR_INVALID_ARGUMENT
+    assert "ASSERT" in lib.gnc_last_error().decode()
+    assert lib.gnc_host_alloc(16, None) == _lib.GNC_ERR_INVALID_ARGUMENT
+    assert lib.gnc_host_free(None) == _lib.GNC_OK
