@@ -51,3 +51,15 @@ def test_get_centre_shapes():
     assert c.shape == (5,) and c.dtype == np.float32 and c[0] == 16.0
     c = api.get_centre((5, 10, 32), 12.5)
     assert c.shape == (5,) and np.all(c == 12.5)
+
+
+def test_public_functions_refuse_the_cpu_path():
+    """No CPU fallback behind the public functions: device="cpu" (the
+    reference's default) raises instead of computing on the host."""
+    import guanaco_gb300 as G
+
+    proj = np.zeros((3, 4, 8), np.float32)
+    with pytest.raises(RuntimeError, match="device path only"):
+        G.reconstruct(proj, np.zeros(3, np.float32), device="cpu")
+    with pytest.raises(RuntimeError, match="device path only"):
+        G.correct_projections(proj, device="cpu")
