@@ -97,3 +97,97 @@ def test_cpp_interface(tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0, r.stdout + r.stderr
     assert r.stdout.strip().endswith("OK")
+
+
+DEVICE_PROGRAM = r"""
+#include <cstdio>
+#include <vector>
+#include "guanaco_gb300.hpp"
+
+// argv: sinogram file (9 x 32 floats), output reconstruction file (32 x 32),
+// image file (16 x 24 floats), ctf file (2 x 16 x 24 complex), output corrected file
+static std::vector<float> read(const char *path, size_t n) {
+  std::vector<float> v(n);
+  FILE *f = std::fopen(path, "rb");
+  if (!f || std::fread(v.data(), sizeof(float), n, f) != n) throw guanaco::Error("read");
+  std::fclose(f);
+  return v;
+}
+static void write(const char *path, const std::vector<float> &v) {
+  FILE *f = std::fopen(path, "wb");
+  std::fwrite(v.data(), sizeof(float), v.size(), f);
+  std::fclose(f);
+}
+
+int main(int argc, char **argv) {
+  if (argc != 6) return 2;
+  try {
+    guanaco::Config c;
+    c.device = guanaco::e_device;
+    c.gpu_index = -1;
+    c.num_pixels = 32; c.num_angles = 9; c.num_defocus = 1;
+    c.grid_height = 32; c.grid_width = 32;
+    c.centre = 16.f;
+    for (int t = 0; t < 9; ++t) c.angles.push_back(-1.f + 0.25f * t);
+    std::vector<float> sino = read(argv[1], 9 * 32), rec(32 * 32, -1.f);
+    guanaco::make_reconstructor(c)(sino.data(), rec.data());
+    write(argv[2], rec);
+    std::vector<float> image = read(argv[3], 16 * 24), ctf = read(argv[4], 2 * 16 * 24 * 2);
+    std::vector<float> out(2 * 16 * 24);
+    guanaco::correct<float>(image.data(), reinterpret_cast<const std::complex<float> *>(ctf.data()),
+                            out.data(), 24, 16, 2, guanaco::e_device);
+    write(argv[5], out);
+  } catch (const guanaco::Error &e) {
+    std::printf("Error: %s\n", e.what());
+    return 1;
+  }
+  return 0;
+}
+"""
+
+
+@pytest.mark.gpu
+def test_cpp_device_calls_match_python(tmp_path):
+    """Reconstructor and correct<float> of the C++ interface give exactly the
+    volumes of guanaco_gb300.detail.recon and corr (the same C ABI calls)."""
+    import numpy as np
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA device")
+    from guanaco_gb300 import _lib, detail
+
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    lib = _lib.lib_path()
+    _lib.load()
+    src = tmp_path / "dev.cpp"
+    src.write_text(DEVICE_PROGRAM)
+    exe = tmp_path / "dev"
+    libdir = os.path.dirname(lib)
+    subprocess.run([gxx, "-std=c++11", "-Wall", "-I", os.path.join(REPO, "include"), str(src),
+                    "-o", str(exe), "-L", libdir, "-lguanaco_gb300", "-Wl,-rpath," + libdir],
+                   check=True, capture_output=True, text=True)
+    rng = np.random.default_rng(3)
+    sino = rng.standard_normal((9, 32)).astype(np.float32)
+    image = rng.standard_normal((16, 24)).astype(np.float32)
+    ctf = (rng.standard_normal((2, 16, 24)) + 1j * rng.standard_normal((2, 16, 24))).astype(
+        np.complex64)
+    paths = [tmp_path / n for n in ("sino", "rec", "image", "ctf", "corr")]
+    sino.tofile(paths[0])
+    image.tofile(paths[2])
+    ctf.tofile(paths[3])
+    r = subprocess.run([str(exe)] + [str(p) for p in paths], capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    got_rec = np.fromfile(paths[1], np.float32).reshape(32, 32)
+    got_corr = np.fromfile(paths[4], np.float32).reshape(2, 16, 24)
+    ang = (-1.0 + 0.25 * np.arange(9)).astype(np.float32)
+    want_rec = np.empty((32, 32), np.float32)
+    detail.recon(sino, want_rec, ang, 16.0, device="gpu")
+    want_corr = np.empty((2, 16, 24), np.float32)
+    detail.corr(image, ctf, want_corr, device="gpu")
+    np.testing.assert_array_equal(got_rec, want_rec)
+    np.testing.assert_array_equal(got_corr, want_corr)
+    assert np.abs(want_rec).max() > 0 and np.abs(want_corr).max() > 0
