@@ -10,7 +10,11 @@
  *   guanaco::Reconstructor(_t) include/guanaco/reconstructor.h:26-59
  *   guanaco::Filter           include/guanaco/filter.h:32-54
  *   guanaco::correct          include/guanaco/correct.h:77-95
- * and the CTF unit conversions of include/guanaco/ctf.h.  Only e_device runs:
+ *   guanaco::CTF              include/guanaco/ctf.h:167-178, with get_chi,
+ *                             get_ctf(_simple(_real|_imag)), get_Es_n,
+ *                             get_Et_n, the get_ctf_n* grids and the unit
+ *                             conversions of include/guanaco/ctf.h.
+ * Only e_device runs:
  * an e_host object or call throws guanaco::Error, as there is no CPU path
  * behind this library (the reference's own host code remains the CPU path).
  * A failed call throws guanaco::Error with gnc_last_error(); argument checks
@@ -209,6 +213,126 @@ void correct(const T *image, const std::complex<T> *ctf, T *rec, std::size_t xsi
   gb300_detail::require_device(device, "correct");
   gb300_detail::check(gnc_correct(image, reinterpret_cast<const float *>(ctf), rec, xsize, ysize,
                                   num_ctf));
+}
+
+// CTF parameters (include/guanaco/ctf.h:167-178) and their evaluation through
+// the library's CTF physics (double precision, as the reference evaluates
+// them): chi, the full CTF with envelopes, the simple CTF and its parts, the
+// envelopes element-wise, and FFT-ordered grids at pixel size ps.
+struct CTF {
+  double l;        // wavelength (A)
+  double df;       // defocus (A)
+  double Cs;       // spherical aberration (A)
+  double Ca;       // 2-fold astigmatism (A)
+  double Pa;       // angle of 2-fold astigmatism (rad)
+  double dd;       // defocus spread (A)
+  double theta_c;  // source spread (rad)
+  double phi;      // phase shift (rad)
+
+  CTF() : l(0), df(0), Cs(0), Ca(0), Pa(0), dd(0), theta_c(0), phi(0) {}
+};
+
+namespace gb300_detail {
+
+inline gnc_ctf to_c(const CTF &c) {
+  gnc_ctf g;
+  g.l = c.l;
+  g.df = c.df;
+  g.Cs = c.Cs;
+  g.Ca = c.Ca;
+  g.Pa = c.Pa;
+  g.dd = c.dd;
+  g.theta_c = c.theta_c;
+  g.phi = c.phi;
+  return g;
+}
+
+// one (q, theta) of a kind: out[0] (real kinds) or out[0] + i out[1]
+inline void eval1(const CTF &c, int kind, double q, double theta, double *out) {
+  const gnc_ctf g = to_c(c);
+  check(gnc_ctf_eval(&g, kind, &q, &theta, 1, out));
+}
+
+// an (h, w) grid of a complex or a real kind, converted to the caller's
+// element type
+template <typename U>
+void grid_complex(const CTF &c, int kind, U *out, std::size_t w, std::size_t h, double ps) {
+  std::vector<double> tmp(2 * w * h);
+  const gnc_ctf g = to_c(c);
+  check(gnc_ctf_grid(&g, kind, w, h, ps, tmp.data()));
+  for (std::size_t i = 0; i < w * h; ++i) out[i] = U(tmp[2 * i], tmp[2 * i + 1]);
+}
+
+template <typename U>
+void grid_real(const CTF &c, int kind, U *out, std::size_t w, std::size_t h, double ps) {
+  std::vector<double> tmp(w * h);
+  const gnc_ctf g = to_c(c);
+  check(gnc_ctf_grid(&g, kind, w, h, ps, tmp.data()));
+  for (std::size_t i = 0; i < w * h; ++i) out[i] = U(tmp[i]);
+}
+
+}  // namespace gb300_detail
+
+inline double get_chi(const CTF &c, double q, double theta) {
+  const gnc_ctf g = gb300_detail::to_c(c);
+  return gnc_ctf_chi(&g, q, theta);
+}
+
+inline std::complex<double> get_ctf(const CTF &c, double q, double theta) {
+  double v[2];
+  gb300_detail::eval1(c, GNC_CTF_FULL, q, theta, v);
+  return std::complex<double>(v[0], v[1]);
+}
+
+inline std::complex<double> get_ctf_simple(const CTF &c, double q, double theta) {
+  double v[2];
+  gb300_detail::eval1(c, GNC_CTF_SIMPLE, q, theta, v);
+  return std::complex<double>(v[0], v[1]);
+}
+
+inline double get_ctf_simple_real(const CTF &c, double q, double theta) {
+  double v;
+  gb300_detail::eval1(c, GNC_CTF_SIMPLE_REAL, q, theta, &v);
+  return v;
+}
+
+inline double get_ctf_simple_imag(const CTF &c, double q, double theta) {
+  double v;
+  gb300_detail::eval1(c, GNC_CTF_SIMPLE_IMAG, q, theta, &v);
+  return v;
+}
+
+// spatial and temporal coherence envelopes of n frequencies
+inline void get_Es_n(const CTF &c, const double *q, const double *theta, double *Es,
+                     std::size_t n) {
+  const gnc_ctf g = gb300_detail::to_c(c);
+  gb300_detail::check(gnc_ctf_eval(&g, GNC_CTF_ES, q, theta, n, Es));
+}
+
+inline void get_Et_n(const CTF &c, const double *q, double *Et, std::size_t n) {
+  const gnc_ctf g = gb300_detail::to_c(c);
+  gb300_detail::check(gnc_ctf_eval(&g, GNC_CTF_ET, q, nullptr, n, Et));
+}
+
+// FFT-ordered (h, w) grids at pixel size ps (include/guanaco/ctf.h:466-557)
+template <typename T, typename U = std::complex<T>>
+void get_ctf_n(const CTF &c, U *ctf, std::size_t w, std::size_t h, T ps) {
+  gb300_detail::grid_complex(c, GNC_CTF_FULL, ctf, w, h, (double)ps);
+}
+
+template <typename T, typename U = std::complex<T>>
+void get_ctf_n_simple(const CTF &c, U *ctf, std::size_t w, std::size_t h, T ps) {
+  gb300_detail::grid_complex(c, GNC_CTF_SIMPLE, ctf, w, h, (double)ps);
+}
+
+template <typename T>
+void get_ctf_n_simple_real(const CTF &c, T *ctf, std::size_t w, std::size_t h, T ps) {
+  gb300_detail::grid_real(c, GNC_CTF_SIMPLE_REAL, ctf, w, h, (double)ps);
+}
+
+template <typename T>
+void get_ctf_n_simple_imag(const CTF &c, T *ctf, std::size_t w, std::size_t h, T ps) {
+  gb300_detail::grid_real(c, GNC_CTF_SIMPLE_IMAG, ctf, w, h, (double)ps);
 }
 
 // CTF unit conversions (include/guanaco/ctf.h), double precision.

@@ -191,3 +191,99 @@ def test_cpp_device_calls_match_python(tmp_path):
     np.testing.assert_array_equal(got_rec, want_rec)
     np.testing.assert_array_equal(got_corr, want_corr)
     assert np.abs(want_rec).max() > 0 and np.abs(want_corr).max() > 0
+
+
+CTF_PROGRAM = r"""
+#include <cstdio>
+#include <vector>
+#include "guanaco_gb300.hpp"
+
+// writes the reference's CTF known answers, evaluated through the C++
+// interface, to argv[1] as raw doubles in a fixed order
+int main(int argc, char **argv) {
+  if (argc != 2) return 2;
+  std::vector<double> out;
+  const double l = guanaco::get_electron_wavelength(300000);
+  guanaco::CTF c;
+  c.l = l; c.df = 20000; c.Cs = 2.7e7;
+  out.push_back(guanaco::get_chi(c, 10, 0));
+  guanaco::CTF env = c;
+  env.dd = 1; env.theta_c = 1e-3;
+  double q = 10, theta = 0, Es = 0, Et = 0;
+  guanaco::get_Es_n(env, &q, &theta, &Es, 1);
+  guanaco::get_Et_n(env, &q, &Et, 1);
+  out.push_back(Es);
+  out.push_back(Et);
+  guanaco::CTF full = c;
+  full.dd = 1; full.theta_c = 0.1 / 1e3; full.phi = 0.1;
+  std::vector<std::complex<double>> g(100 * 100);
+  guanaco::get_ctf_n(full, g.data(), 100, 100, 2.0);
+  for (auto v : g) { out.push_back(v.real()); out.push_back(v.imag()); }
+  guanaco::CTF simple = c;
+  simple.phi = 0.1;
+  guanaco::get_ctf_n_simple(simple, g.data(), 100, 100, 2.0);
+  for (auto v : g) { out.push_back(v.real()); out.push_back(v.imag()); }
+  std::vector<double> r(100 * 100);
+  guanaco::get_ctf_n_simple_real(simple, r.data(), 100, 100, 2.0);
+  out.insert(out.end(), r.begin(), r.end());
+  guanaco::get_ctf_n_simple_imag(simple, r.data(), 100, 100, 2.0);
+  out.insert(out.end(), r.begin(), r.end());
+  guanaco::CTF astig = c;
+  astig.df = 25000; astig.Ca = 800; astig.Pa = 0.3; astig.phi = 0.05;
+  std::vector<std::complex<double>> a(90 * 64);
+  guanaco::get_ctf_n_simple(astig, a.data(), 90, 64, 1.5);
+  for (auto v : a) { out.push_back(v.real()); out.push_back(v.imag()); }
+  // the scalar forms agree with the grid forms
+  const std::complex<double> s = guanaco::get_ctf_simple(simple, 0.05, 0.3);
+  out.push_back(s.real() - guanaco::get_ctf_simple_real(simple, 0.05, 0.3));
+  out.push_back(s.imag() - guanaco::get_ctf_simple_imag(simple, 0.05, 0.3));
+  FILE *f = std::fopen(argv[1], "wb");
+  std::fwrite(out.data(), sizeof(double), out.size(), f);
+  std::fclose(f);
+  return 0;
+}
+"""
+
+
+def test_cpp_ctf_known_answers(tmp_path):
+    """guanaco::CTF and its evaluation functions reproduce the reference's CTF
+    known answers (tests/golden/ctf_kat.npz, recorded from the reference)."""
+    import numpy as np
+
+    from conftest import golden
+    from guanaco_gb300 import _lib
+
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    lib = _lib.lib_path()
+    _lib.load()
+    src = tmp_path / "ctf.cpp"
+    src.write_text(CTF_PROGRAM)
+    exe = tmp_path / "ctf"
+    libdir = os.path.dirname(lib)
+    subprocess.run([gxx, "-std=c++11", "-Wall", "-Werror", "-I", os.path.join(REPO, "include"),
+                    str(src), "-o", str(exe), "-L", libdir, "-lguanaco_gb300",
+                    "-Wl,-rpath," + libdir], check=True, capture_output=True, text=True)
+    out = tmp_path / "ctf.bin"
+    r = subprocess.run([str(exe), str(out)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
+    v = np.fromfile(out, np.float64)
+    g = golden("ctf_kat")
+    n = 100 * 100
+    chi, es, et = v[0], v[1], v[2]
+    o = 3
+    full = v[o:o + 2 * n].view(np.complex128).reshape(100, 100); o += 2 * n
+    simple = v[o:o + 2 * n].view(np.complex128).reshape(100, 100); o += 2 * n
+    real = v[o:o + n].reshape(100, 100); o += n
+    imag = v[o:o + n].reshape(100, 100); o += n
+    astig = v[o:o + 2 * 90 * 64].view(np.complex128).reshape(64, 90); o += 2 * 90 * 64
+    assert chi == pytest.approx(float(g["chi_q10"]), rel=1e-15)
+    np.testing.assert_allclose([es], g["Es_q10"], rtol=1e-14)
+    np.testing.assert_allclose([et], g["Et_q10"], rtol=1e-14)
+    np.testing.assert_allclose(full, g["ctf_full"], rtol=0, atol=1e-13)
+    np.testing.assert_array_equal(simple, g["ctf_simple"])
+    np.testing.assert_array_equal(real, g["ctf_simple_real"])
+    np.testing.assert_array_equal(imag, g["ctf_simple_imag"])
+    np.testing.assert_array_equal(astig, g["ctf_simple_astig_90x64"])
+    assert v[o] == 0.0 and v[o + 1] == 0.0 and o + 2 == v.size
