@@ -189,7 +189,7 @@ void fail(gnc_server *S, Request *r, int status, const std::string &msg) {
 }
 
 // Without the lock: plan, buffers and parameter block of a new cache entry.
-int create_entry(gnc_server *S, Cached *c, const Request *r) {
+int create_entry(Cached *c, const Request *r) {
   int st = gnc_fbp_plan_create(&r->desc, &c->plan);
   if (st != GNC_OK) return st;
   cudaError_t e = cudaMalloc((void **)&c->d_in, r->in_bytes);
@@ -353,7 +353,7 @@ void build_loop(gnc_server *S) {
     for (auto &v : b.victims) release(v.get());
     b.victims.clear();
     std::string msg;
-    int st = create_entry(S, b.c, b.r);
+    int st = create_entry(b.c, b.r);
     if (st != GNC_OK) msg = gnc::last_error();
     if (st == GNC_OK) {
       st = enqueue(S, b.sl, b.r, b.c, true);
