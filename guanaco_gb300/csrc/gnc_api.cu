@@ -17,6 +17,7 @@
 
 #include "../../include/guanaco_gb300.h"
 #include "gnc_common.cuh"
+#include "gnc_host_geom.h"
 #include "gnc_plan_hooks.h"
 
 namespace gnc {
@@ -52,6 +53,14 @@ bool fft_length_supported(long n) {
   return n >= 1 && factorize(n, r, &ns);
 }
 
+bool make_fft_factors(int n, FftPlan *out) {
+  FftPlan p{};
+  p.n = n;
+  if (!factorize(n, p.radix, &p.nstage)) return false;
+  *out = p;
+  return true;
+}
+
 bool make_fft_plan(int n, FftPlan *out) {
   FftPlan p{};
   p.n = n;
@@ -82,33 +91,6 @@ bool make_fft_plan(int n, FftPlan *out) {
   p.roots = it->second;
   *out = p;
   return true;
-}
-
-// ------------------------------------------------------- host geometry -----
-// reconstructor.cpp:35-47 (float arithmetic, std::cos/std::sin of float).
-static TiltGeom tilt_geometry(float theta, float centre, size_t num_angles, float *offset) {
-  double output_scale = M_PI / (double)(2 * num_angles);
-  float cos_angle = std::cos(theta);
-  float sin_angle = std::sin(theta);
-  float det_x0 = -centre * cos_angle;
-  float det_y0 = -centre * sin_angle;
-  float ray_length = std::sqrt(cos_angle * cos_angle + sin_angle * sin_angle);
-  float d = cos_angle * cos_angle + sin_angle * sin_angle;
-  TiltGeom g;
-  *offset = (det_y0 * (-sin_angle) - det_x0 * cos_angle) / d;
-  g.scale = (float)(output_scale * ray_length / std::abs(d));
-  g.cos_a = cos_angle / d;
-  g.sin_a = sin_angle / d;
-  g.pad = 0.f;
-  return g;
-}
-
-// reconstructor.cpp:28-32 / reconstructor.cu:253-256
-static void defocus_scale(size_t num_defocus, float pixel_size, float min_defocus,
-                          float max_defocus, float *dscale, float *doffset) {
-  float ds = num_defocus > 1 ? (float)num_defocus * pixel_size / (max_defocus - min_defocus) : 0.0f;
-  *dscale = ds;
-  *doffset = -ds * (min_defocus / pixel_size);
 }
 
 }  // namespace gnc
@@ -406,6 +388,47 @@ int plan_set_request(gnc_fbp_plan *p, const gnc_fbp_desc *d, unsigned char *host
 }
 
 int *plan_error_word(gnc_fbp_plan *p) { return p->err; }
+
+}  // namespace gnc
+
+// ------------------------------------------------ shared request checks ---
+namespace gnc {
+
+#define GNC_CONFIG_REQUIRE(cond)                                              \
+  do {                                                                        \
+    if (!(cond)) {                                                            \
+      set_error(std::string(who) + ": ASSERT (" #cond ") failed");            \
+      return GNC_ERR_INVALID_ARGUMENT;                                        \
+    }                                                                         \
+  } while (0)
+
+int config_check(const gnc_config *c, const char *who) {
+  GNC_CONFIG_REQUIRE(c != nullptr);
+  if (c->device != 1) {
+    set_error(std::string(who) + ": guanaco_gb300 implements the device path (device = gpu) only");
+    return GNC_ERR_UNSUPPORTED;
+  }
+  // Config::is_valid (config.h:66-75)
+  GNC_CONFIG_REQUIRE(c->num_pixels > 0);
+  GNC_CONFIG_REQUIRE(c->num_angles > 0);
+  GNC_CONFIG_REQUIRE(c->num_defocus > 0);
+  GNC_CONFIG_REQUIRE(c->grid_height > 0);
+  GNC_CONFIG_REQUIRE(c->grid_width > 0);
+  GNC_CONFIG_REQUIRE(c->pixel_size > 0);
+  GNC_CONFIG_REQUIRE(c->min_defocus <= c->max_defocus);
+  GNC_CONFIG_REQUIRE(c->angles != nullptr);
+  // BP::launch (reconstructor.cu:250)
+  GNC_CONFIG_REQUIRE(c->num_defocus == 1 || c->max_defocus > c->min_defocus);
+  if (c->num_pixels > 6400 || !fft_length_supported(2 * (long)c->num_pixels)) {
+    set_error(std::string(who) +
+              ": unsupported num_pixels: 2 * num_pixels must factorise into radices <= 16 "
+              "and num_pixels <= 6400");
+    return GNC_ERR_UNSUPPORTED;
+  }
+  return GNC_OK;
+}
+
+#undef GNC_CONFIG_REQUIRE
 
 }  // namespace gnc
 
@@ -834,31 +857,6 @@ static int select_device(int gpu_index) {
   return GNC_OK;
 }
 
-static int check_config(const gnc_config *c) {
-  GNC_REQUIRE(c != nullptr);
-  if (c->device != 1) {
-    set_error("guanaco_gb300 implements the device path (device = gpu) only");
-    return GNC_ERR_UNSUPPORTED;
-  }
-  // Config::is_valid (config.h:66-75)
-  GNC_REQUIRE(c->num_pixels > 0);
-  GNC_REQUIRE(c->num_angles > 0);
-  GNC_REQUIRE(c->num_defocus > 0);
-  GNC_REQUIRE(c->grid_height > 0);
-  GNC_REQUIRE(c->grid_width > 0);
-  GNC_REQUIRE(c->pixel_size > 0);
-  GNC_REQUIRE(c->min_defocus <= c->max_defocus);
-  GNC_REQUIRE(c->angles != nullptr);
-  // BP::launch (reconstructor.cu:250)
-  GNC_REQUIRE(c->num_defocus == 1 || c->max_defocus > c->min_defocus);
-  if (c->num_pixels > 6400 || !fft_length_supported(2 * (long)c->num_pixels)) {
-    set_error("unsupported num_pixels: 2 * num_pixels must factorise into radices <= 16 "
-              "and num_pixels <= 6400");
-    return GNC_ERR_UNSUPPORTED;
-  }
-  return GNC_OK;
-}
-
 int gnc_filter_device(size_t num_pixels, size_t num_angles, size_t num_defocus, float *d_data,
                       void *stream) {
   // Filter<e_device>::Filter asserts (filter.cu:139-141)
@@ -889,7 +887,7 @@ int gnc_filter_device(size_t num_pixels, size_t num_angles, size_t num_defocus, 
 }
 
 int gnc_reconstruct_device(const gnc_config *c, const float *d_sino, float *d_rec, void *stream) {
-  int st = check_config(c);
+  int st = config_check(c, "gnc_reconstruct_device");
   if (st != GNC_OK) return st;
   GNC_REQUIRE(d_sino != nullptr && d_rec != nullptr);
   cudaStream_t s = (cudaStream_t)stream;
@@ -935,7 +933,7 @@ int gnc_reconstruct_device(const gnc_config *c, const float *d_sino, float *d_re
 }
 
 int gnc_reconstruct(const gnc_config *c, const float *sinogram, float *reconstruction) {
-  int st = check_config(c);
+  int st = config_check(c, "gnc_reconstruct");
   if (st != GNC_OK) return st;
   GNC_REQUIRE(sinogram != nullptr && reconstruction != nullptr);
   st = select_device(c->gpu_index);

@@ -5,7 +5,6 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include <atomic>
 #include <string>
 
 #include "gnc_fft.cuh"
@@ -20,6 +19,9 @@ const char *last_error();
 // Returns false (and sets the error) when n has a prime factor > kMaxRadix.
 bool make_fft_plan(int n, FftPlan *out);
 bool fft_length_supported(long n);
+// The factorisation only (roots left null, nothing allocated); false when n
+// has a prime factor > kMaxRadix.
+bool make_fft_factors(int n, FftPlan *out);
 
 // ---- staging element types ------------------------------------------------
 enum Staging : int { kStageF32 = 0, kStageF16 = 1 };
@@ -129,20 +131,13 @@ struct RowStageArgs {
 };
 cudaError_t launch_row_stage(const RowStageArgs &a, cudaStream_t s);
 
-// Raises a kernel's dynamic shared-memory limit once per device: the
-// attribute belongs to the current device's context, so a process that
-// launches on several GPUs sets it on each (one flag bit per device ordinal).
+// Raises a kernel's dynamic shared-memory limit on the current device.  The
+// attribute belongs to the device's context, so it is set before every launch
+// (a cheap host call): a process that launches on several GPUs, or whose
+// context was torn down and rebuilt, gets it on the context it launches in.
 template <auto KERNEL>
 inline cudaError_t ensure_dynamic_smem(int bytes) {
-  static std::atomic<unsigned long long> done{0ull};
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  const unsigned long long bit = 1ull << (dev & 63);
-  if (done.load(std::memory_order_acquire) & bit) return cudaSuccess;
-  e = cudaFuncSetAttribute(KERNEL, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  if (e == cudaSuccess) done.fetch_or(bit, std::memory_order_release);
-  return e;
+  return cudaFuncSetAttribute(KERNEL, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 // Row pairs a row-stage launch covers: rows 2 y2_begin .. of every (tilt, slab).
 __host__ __device__ inline int row_pairs(const RowStageArgs &a) {

@@ -13,20 +13,24 @@
 //
 // Consequences for callers:
 //  * limits: num_defocus * num_angles * num_pixels <= 4 Mi floats,
-//    num_angles <= 1024, num_pixels <= 4096 (the zero-padded row length
-//    2 * num_pixels must also factorise into radices <= 16); larger requests
-//    are rejected with GNC_ERR_INVALID_ARGUMENT and a message naming the limit;
+//    num_angles <= 1024, num_pixels <= 4096; larger requests are rejected
+//    with GNC_ERR_INVALID_ARGUMENT and a message naming the limit.  Requests
+//    the allocating entry point would reject are rejected here with the same
+//    status (the same checks, gnc_host_geom.h);
 //  * all calls on one device share the arrays, which keep the last call's
 //    contents: calls that may overlap on the GPU (different streams, or host
 //    threads racing) race on them and must be serialised by the caller;
-//  * the first call on a device looks up the arrays' device addresses
-//    (cudaGetSymbolAddress with that device current) and keeps them.
+//  * every call looks up the arrays' device addresses on the current device
+//    (cudaGetSymbolAddress, which allocates nothing), so a context torn down
+//    and rebuilt (cudaDeviceReset) cannot leave it stale pointers.  The first
+//    call on a device is its set-up: that lookup loads this library's device
+//    code there, which is when the arrays come into existence, so the first
+//    call should come before any stream capture on that device.
 #include <math.h>
-
-#include <mutex>
 
 #include "../../include/guanaco_gb300.h"
 #include "gnc_common.cuh"
+#include "gnc_host_geom.h"
 
 namespace gnc {
 namespace {
@@ -46,60 +50,28 @@ struct DeviceScratch {
   float *sino = nullptr;
   TiltGeom *geom = nullptr;
   float2 *roots = nullptr;
-  bool ready = false;
 };
-constexpr int kMaxDevices = 64;
-static DeviceScratch g_scratch[kMaxDevices];
-static std::mutex g_scratch_lock;
 
-// Device addresses of the scratch arrays on the current device (first call
-// per device looks them up).
+// Device addresses of the scratch arrays on the current device, looked up on
+// every call (a lookup is a table search in the runtime, not an allocation).
 static int scratch_for_current_device(DeviceScratch *out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_sino);
+  if (e == cudaSuccess) {
+    out->sino = (float *)p;
+    e = cudaGetSymbolAddress(&p, g_geom);
+  }
+  if (e == cudaSuccess) {
+    out->geom = (TiltGeom *)p;
+    e = cudaGetSymbolAddress(&p, g_roots);
+  }
   if (e != cudaSuccess) {
-    set_error(std::string("gnc_reconstruct_device_noalloc: cudaGetDevice: ") +
+    set_error(std::string("gnc_reconstruct_device_noalloc: cudaGetSymbolAddress: ") +
               cudaGetErrorString(e));
     return GNC_ERR_CUDA;
   }
-  if (dev < 0 || dev >= kMaxDevices) {
-    set_error("gnc_reconstruct_device_noalloc: device index beyond 64");
-    return GNC_ERR_UNSUPPORTED;
-  }
-  std::lock_guard<std::mutex> lk(g_scratch_lock);
-  DeviceScratch &s = g_scratch[dev];
-  if (!s.ready) {
-    void *p = nullptr;
-    if ((e = cudaGetSymbolAddress(&p, g_sino)) != cudaSuccess) goto fail;
-    s.sino = (float *)p;
-    if ((e = cudaGetSymbolAddress(&p, g_geom)) != cudaSuccess) goto fail;
-    s.geom = (TiltGeom *)p;
-    if ((e = cudaGetSymbolAddress(&p, g_roots)) != cudaSuccess) goto fail;
-    s.roots = (float2 *)p;
-    s.ready = true;
-  }
-  *out = s;
+  out->roots = (float2 *)p;
   return GNC_OK;
-fail:
-  set_error(std::string("gnc_reconstruct_device_noalloc: cudaGetSymbolAddress: ") +
-            cudaGetErrorString(e));
-  return GNC_ERR_CUDA;
-}
-
-static bool factor_radices(int n, FftPlan *p) {
-  int ns = 0;
-  while (n % 8 == 0) { p->radix[ns++] = 8; n /= 8; }
-  while (n % 4 == 0) { p->radix[ns++] = 4; n /= 4; }
-  while (n % 2 == 0) { p->radix[ns++] = 2; n /= 2; }
-  for (int f = 3; n > 1; f += 2) {
-    while (n % f == 0) {
-      if (f > kMaxRadix || ns >= kMaxStages) return false;
-      p->radix[ns++] = f;
-      n /= f;
-    }
-  }
-  p->nstage = ns;
-  return true;
 }
 
 // exp(-2 pi i k / L) in double, rounded to float.
@@ -159,35 +131,29 @@ using namespace gnc;
 
 extern "C" int gnc_reconstruct_device_noalloc(const gnc_config *c, const float *d_sino,
                                               float *d_rec, void *stream) {
-  if (!c || !d_sino || !d_rec) {
-    set_error("gnc_reconstruct_device_noalloc: null config or buffer");
+  // the allocating entry point's checks first, with its statuses
+  const int valid = config_check(c, "gnc_reconstruct_device_noalloc");
+  if (valid != GNC_OK) return valid;
+  if (!d_sino || !d_rec) {
+    set_error("gnc_reconstruct_device_noalloc: ASSERT (d_sino != nullptr && d_rec != nullptr) "
+              "failed");
     return GNC_ERR_INVALID_ARGUMENT;
   }
-  if (c->device != 1) {
-    set_error("gnc_reconstruct_device_noalloc: the device path (device = gpu) only");
-    return GNC_ERR_UNSUPPORTED;
-  }
-  // guanaco::Config::is_valid (config.h:66-75) and BP::launch (reconstructor.cu:250)
-  if (!(c->num_pixels > 0 && c->num_angles > 0 && c->num_defocus > 0 && c->grid_height > 0 &&
-        c->grid_width > 0 && c->pixel_size > 0 && c->min_defocus <= c->max_defocus &&
-        c->angles != nullptr && (c->num_defocus == 1 || c->max_defocus > c->min_defocus))) {
-    set_error("gnc_reconstruct_device_noalloc: invalid configuration (guanaco::Config::is_valid)");
-    return GNC_ERR_INVALID_ARGUMENT;
-  }
-  const size_t sino = c->num_pixels * c->num_angles * c->num_defocus;
-  if (sino > kMaxSino || c->num_angles > (size_t)kMaxTilts ||
-      c->num_pixels > (size_t)kMaxPixels) {
+  // then the static scratch's limits, each factor on its own so that the
+  // product below cannot wrap
+  if (c->num_angles > (size_t)kMaxTilts || c->num_pixels > (size_t)kMaxPixels ||
+      c->num_defocus > kMaxSino / (c->num_angles * c->num_pixels)) {
     set_error("gnc_reconstruct_device_noalloc: request exceeds the static scratch "
               "(num_defocus * num_angles * num_pixels <= 4194304, num_angles <= 1024, "
               "num_pixels <= 4096)");
     return GNC_ERR_INVALID_ARGUMENT;
   }
+  const size_t sino = c->num_pixels * c->num_angles * c->num_defocus;
   const int N = (int)c->num_pixels, L = 2 * N;
   FftPlan plan{};
-  plan.n = L;
-  if (!factor_radices(L, &plan)) {
-    set_error("gnc_reconstruct_device_noalloc: 2 * num_pixels must factorise into radices <= 16");
-    return GNC_ERR_INVALID_ARGUMENT;
+  if (!make_fft_factors(L, &plan)) {  // config_check has accepted this length
+    set_error("gnc_reconstruct_device_noalloc: 2 * num_pixels does not factorise");
+    return GNC_ERR_UNSUPPORTED;
   }
   DeviceScratch s;
   int st = scratch_for_current_device(&s);
@@ -198,23 +164,10 @@ extern "C" int gnc_reconstruct_device_noalloc(const gnc_config *c, const float *
   // per-tilt geometry with the reference's float arithmetic (reconstructor.cpp:35-47)
   TiltGeom geom[kMaxTilts];
   float offset = 0.f;
-  const double output_scale = M_PI / (double)(2 * c->num_angles);
-  for (size_t t = 0; t < c->num_angles; ++t) {
-    const float theta = c->angles[t];
-    const float ca = cosf(theta), sa = sinf(theta);
-    const float det_x0 = -c->centre * ca, det_y0 = -c->centre * sa;
-    const float ray = sqrtf(ca * ca + sa * sa);
-    const float d = ca * ca + sa * sa;
-    offset = (det_y0 * (-sa) - det_x0 * ca) / d;
-    geom[t].scale = (float)(output_scale * ray / fabsf(d));
-    geom[t].cos_a = ca / d;
-    geom[t].sin_a = sa / d;
-    geom[t].pad = 0.f;
-  }
-  const float dscale = c->num_defocus > 1
-                           ? (float)c->num_defocus * c->pixel_size / (c->max_defocus - c->min_defocus)
-                           : 0.0f;
-  const float doffset = -dscale * (c->min_defocus / c->pixel_size);
+  for (size_t t = 0; t < c->num_angles; ++t)
+    geom[t] = tilt_geometry(c->angles[t], c->centre, c->num_angles, &offset);
+  float dscale, doffset;
+  defocus_scale(c->num_defocus, c->pixel_size, c->min_defocus, c->max_defocus, &dscale, &doffset);
 
   cudaError_t e = cudaMemcpyAsync(s.geom, geom, c->num_angles * sizeof(TiltGeom),
                                   cudaMemcpyHostToDevice, strm);
@@ -231,7 +184,9 @@ extern "C" int gnc_reconstruct_device_noalloc(const gnc_config *c, const float *
     const int npair = (nrows + 1) / 2;
     if (rp > npair) rp = npair;
     const size_t smem = 2ull * rp * L * sizeof(float2);
-    e = ensure_dynamic_smem<k_noalloc_ramp>(200 * 1024);
+    // set on every call: the attribute belongs to the current context
+    e = cudaFuncSetAttribute(k_noalloc_ramp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             200 * 1024);
     if (e == cudaSuccess) {
       k_noalloc_ramp<<<(npair + rp - 1) / rp, 256, smem, strm>>>(s.sino, nrows, N, plan, rp);
       e = cudaGetLastError();

@@ -85,9 +85,13 @@ GNC_API int gnc_reconstruct_device(const gnc_config *config, const float *d_sino
  * in static device arrays (about 16.1 MiB held by every GPU that loads the
  * library until exit).  Limits: num_defocus * num_angles * num_pixels <=
  * 4194304, num_angles <= 1024, num_pixels <= 4096; larger requests return
- * GNC_ERR_INVALID_ARGUMENT.  All calls on a device share the scratch, so calls
- * that overlap on the GPU race; serialise them.  The first call on a device
- * looks up the scratch's device addresses (cudaGetSymbolAddress). */
+ * GNC_ERR_INVALID_ARGUMENT (other checks and statuses as for
+ * gnc_reconstruct_device).  All calls on a device share the scratch, so calls
+ * that overlap on the GPU race; serialise them.  Every call looks up the
+ * scratch's device addresses on the current device (cudaGetSymbolAddress,
+ * which allocates nothing); the first call on a device is its set-up, which
+ * loads the library's device code there, so make it before any stream
+ * capture on that device. */
 GNC_API int gnc_reconstruct_device_noalloc(const gnc_config *config, const float *d_sinogram,
                                            float *d_reconstruction, void *stream);
 

@@ -224,3 +224,42 @@ def test_host_alloc_argument_checks(lib):
     assert "ASSERT" in lib.gnc_last_error().decode()
     assert lib.gnc_host_alloc(16, None) == _lib.GNC_ERR_INVALID_ARGUMENT
     assert lib.gnc_host_free(None) == _lib.GNC_OK
+
+
+def test_noalloc_limits_are_checked_on_the_host(lib):
+    """The allocation-free entry point rejects requests beyond its static
+    scratch before any CUDA call, and checks each factor of
+    num_defocus * num_angles * num_pixels on its own: a product that wraps
+    around 2^64 (here to 0) is still rejected instead of reaching the device."""
+    import ctypes
+
+    from guanaco_gb300 import _lib
+
+    ang = np.zeros(1024, np.float32)
+    cfg = _lib.GncConfig()
+    cfg.device = 1
+    cfg.gpu_index = -1
+    cfg.num_pixels = 4096
+    cfg.num_angles = 1024
+    cfg.num_defocus = 1 << 42  # 4096 * 1024 * 2^42 == 2^64
+    cfg.grid_height = 16
+    cfg.grid_width = 16
+    cfg.pixel_size = 1.0
+    cfg.centre = 2048.0
+    cfg.min_defocus = -1.0
+    cfg.max_defocus = 1.0
+    cfg.angles = ang.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    fake = ctypes.c_void_p(16)  # never dereferenced: the checks come first
+    st = lib.gnc_reconstruct_device_noalloc(ctypes.byref(cfg), fake, fake, None)
+    assert st == _lib.GNC_ERR_INVALID_ARGUMENT
+    assert b"static scratch" in lib.gnc_last_error()
+    cfg.num_defocus = 2  # 2 * 4 Mi floats
+    assert lib.gnc_reconstruct_device_noalloc(ctypes.byref(cfg), fake, fake,
+                                              None) == _lib.GNC_ERR_INVALID_ARGUMENT
+    cfg.num_pixels = 34  # 2 * 34 has the prime factor 17: unsupported, as for
+    cfg.num_defocus = 1  # the allocating entry point
+    assert lib.gnc_reconstruct_device_noalloc(ctypes.byref(cfg), fake, fake,
+                                              None) == _lib.GNC_ERR_UNSUPPORTED
+    cfg.device = 0
+    assert lib.gnc_reconstruct_device_noalloc(ctypes.byref(cfg), fake, fake,
+                                              None) == _lib.GNC_ERR_UNSUPPORTED
