@@ -30,7 +30,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+# the reference source tree: the first argument, else GUANACO_REFERENCE, else a
+# "reference" directory beside the repository
+REF = (sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GUANACO_REFERENCE")
+       or os.path.join(os.path.dirname(REPO), "reference"))
 
 
 def load_reference():
