@@ -143,6 +143,8 @@ SIGNATURES = {
     "gnc_fbp_staged": (c_int, [c_void, ctypes.POINTER(c_void), ctypes.POINTER(c_void)]),
     "gnc_fbp_check": (c_int, [c_void, c_void]),
     "gnc_fbp_launches": (c_int, [c_void]),
+    "gnc_fbp_backprojector": (c_int, [c_void]),
+    "gnc_debug_wait_probe": (c_int, [ctypes.c_uint]),
     "gnc_server_create": (c_int, [c_size, c_int, ctypes.POINTER(c_void)]),
     "gnc_server_destroy": (c_int, [c_void]),
     "gnc_server_submit": (c_int, [c_void, ctypes.POINTER(GncFbpDesc), c_void, c_void,

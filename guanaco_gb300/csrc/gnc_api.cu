@@ -8,6 +8,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -114,6 +115,10 @@ using namespace gnc;
     }                                                                        \
   } while (0)
 
+// Test hook of the bounded device waits (gnc_debug_wait_probe): plans copy
+// the value when they are created.
+static std::atomic<unsigned> g_wait_probe{0};
+
 // ------------------------------------------------------------- the plan ----
 // Host-buffer pipeline: input copies in up to kIoGroups tilt groups, volume
 // copies out in up to kIoSlabs row slabs (eight, the last one split in three
@@ -187,6 +192,7 @@ struct gnc_fbp_plan {
   float *offset = nullptr;  // (H, T)
   float *tilt_factor = nullptr;
   int *err = nullptr;        // device error word of the bounded waits
+  unsigned wait_probe = 0;   // gnc_debug_wait_probe's value when the plan was created
   size_t bytes = 0;
   // host-buffer path (gnc_fbp_execute_host), created on its first call
   float *io_in = nullptr, *io_out = nullptr;
@@ -245,6 +251,8 @@ static BpArgs bp_args(const gnc_fbp_plan *p, float *vol) {
   a.vol = vol;
   a.err = p->err;
   a.dyn = p->dyn_bp;
+  a.wait_limit = 0;  // the default bound
+  a.wait_probe = p->wait_probe;
   return a;
 }
 
@@ -445,6 +453,7 @@ int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
   const bool ctf = d->input == GNC_INPUT_RAW && d->correct;
   auto *p = new gnc_fbp_plan();
   cudaGetDevice(&p->device);
+  p->wait_probe = g_wait_probe.load();
   p->T = (int)d->num_angles;
   p->H = (int)d->height;
   p->W = (int)d->width;
@@ -822,6 +831,17 @@ int gnc_fbp_launches(const gnc_fbp_plan *p) {
   const int chunks = (p->T + p->chunk - 1) / p->chunk;
   // sign table (+ its packed copy), row and column transforms, per chunk flip + rows, BP
   return 3 + (sign_pack_used(p->H) ? 1 : 0) + 2 * chunks + 1;
+}
+
+int gnc_fbp_backprojector(const gnc_fbp_plan *p) {
+  if (!p) return -1;
+  if (!p->uniform_centre) return 0;
+  return backproject_fast_variant(bp_args(p, nullptr));
+}
+
+int gnc_debug_wait_probe(unsigned polls) {
+  g_wait_probe.store(polls);
+  return GNC_OK;
 }
 
 int gnc_fbp_check(gnc_fbp_plan *p, void *stream) {

@@ -157,7 +157,12 @@ struct BpArgs {
   float *vol;             // (Y, Z, X)
   int *err;               // device error word (bounded waits that gave up), or null
   const float *dyn;       // device (dscale, doffset) overriding the two above, or null
+  unsigned wait_limit;    // polls before a bulk-copy wait gives up (0: kBpWaitLimit)
+  unsigned wait_probe;    // test hook, 0 = off: see gnc_debug_wait_probe
 };
+// Default poll limit of the backprojector's bounded mbarrier waits (each poll
+// suspends for at most about 2 us, so about 2 s in all).
+constexpr unsigned kBpWaitLimit = 1u << 20;
 // The fast kernel's requirements (shared centre, 16-byte aligned rows, at most
 // four slabs per tile); launch_backproject_fast falls back to the exact kernel.
 bool backproject_fast_supported(const BpArgs &a);

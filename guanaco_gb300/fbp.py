@@ -133,6 +133,12 @@ class FbpPlan(FbpDesc):
     def launches_per_execute(self):
         return self._lib.gnc_fbp_launches(self._h)
 
+    @property
+    def backprojector(self):
+        """0: the exact backprojection kernel; 2 or 4: the fast kernel and its
+        slab capacity per tile."""
+        return self._lib.gnc_fbp_backprojector(self._h)
+
     # ------------------------------------------------------------- running
     def execute(self, inp, vol, stream=None):
         """Device input -> device volume (overwritten), enqueued on ``stream``."""

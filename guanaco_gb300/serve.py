@@ -70,18 +70,24 @@ class Server:
         return rid.value
 
     def wait(self, rid, timeout=None):
-        """Wait for a request; returns its info dict (raises if it failed).
-        Returns None if the timeout passes first."""
+        """Wait for a request; returns its info dict (raises GncError, with the
+        same dict as its ``info``, if it failed).  Returns None if the timeout
+        passes first."""
         info = _lib.GncRequestInfo()
         st = self._lib.gnc_server_wait(self._h, int(rid), -1.0 if timeout is None else timeout,
                                        ctypes.byref(info))
         if st == _lib.GNC_ERR_PENDING:
             return None
         self._live.pop(int(rid), None)
-        _lib.check(st)
-        return {"status": info.status, "graph": bool(info.graph),
-                "device_error": bool(info.device_error), "t_submit": info.t_submit,
-                "t_start": info.t_start, "t_done": info.t_done}
+        out = {"status": info.status, "graph": bool(info.graph),
+               "device_error": bool(info.device_error), "t_submit": info.t_submit,
+               "t_start": info.t_start, "t_done": info.t_done}
+        try:
+            _lib.check(st)
+        except _lib.GncError as e:
+            e.info = out  # the failed request's outcome, e.g. device_error
+            raise
+        return out
 
     def now(self):
         """Seconds on the server clock (the clock of the request times)."""

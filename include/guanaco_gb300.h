@@ -242,6 +242,21 @@ GNC_API int gnc_fbp_slab_map(gnc_fbp_plan *plan, int32_t *d_out, void *stream);
 GNC_API int gnc_fbp_sign_table(gnc_fbp_plan *plan, int8_t *d_out, void *stream);
 /* Number of kernel launches one gnc_fbp_execute enqueues. */
 GNC_API int gnc_fbp_launches(const gnc_fbp_plan *plan);
+/* Which backprojection kernel gnc_fbp_execute runs for this plan: 0 the
+ * exact kernel (rows with different centres, an odd detector width or too
+ * many slabs per tile), else the fast kernel's slab capacity per tile (2 or 4);
+ * -1 for a null plan. */
+GNC_API int gnc_fbp_backprojector(const gnc_fbp_plan *plan);
+/* Test hook of the failure detection, no counterpart in the reference.
+ * polls > 0: plans created afterwards (by gnc_fbp_plan_create and by the
+ * request server) make every fast backprojection launch arm one spare
+ * mbarrier for 16 bytes that no copy delivers and wait on it at most `polls`
+ * polls, so the wait gives up and sets the plan's error word exactly as a lost
+ * bulk copy would (gnc_fbp_check returns GNC_ERR_CUDA, a served request
+ * reports device_error); the volume is still computed, no copy is in flight on
+ * that barrier and the kernel ends normally.  polls = 0 (the default) turns it
+ * off for plans created afterwards. */
+GNC_API int gnc_debug_wait_probe(unsigned polls);
 /* Synchronises `stream` and reports (then clears) a device-side error of the
  * plan's kernels: every wait in them is bounded and records a timeout here
  * instead of hanging. */

@@ -357,11 +357,11 @@ static void set_threads(int nthreads) {
 }
 
 /* correct.py:291-318 (tilt loop calling corr) then mp.py:124-153 per row */
-void gno_fbp_ctf_f(const float *proj, size_t T, size_t H, size_t W, const float *angles,
-                   const float *centre, float pixel_size, const float *ctf, size_t D,
-                   float min_defocus, float max_defocus, const double *weights, int minus,
-                   size_t Z, float *vol, size_t y_begin, size_t y_end, size_t t_begin,
-                   size_t t_end, int nthreads) {
+void gno_fbp_ctf_rows_f(const float *proj, size_t T, size_t H, size_t W, const float *angles,
+                        const float *centre, float pixel_size, const float *ctf, size_t D,
+                        float min_defocus, float max_defocus, const double *weights, int minus,
+                        size_t Z, const size_t *rows, size_t nrows, float *out, size_t t_begin,
+                        size_t t_end, int nthreads) {
   set_threads(nthreads);
   size_t nd = D > 0 ? D : 1;
   size_t img = H * W;
@@ -376,8 +376,8 @@ void gno_fbp_ctf_f(const float *proj, size_t T, size_t H, size_t W, const float 
     stack = corr;
   }
 #pragma omp parallel for schedule(dynamic, 1)
-  for (long yy = (long)y_begin; yy < (long)y_end; ++yy) {
-    size_t y = (size_t)yy;
+  for (long i = 0; i < (long)nrows; ++i) {
+    size_t y = rows[i];
     /* numpy.swapaxes + ascontiguousarray: sino (D, T, W) for row y */
     float *sino = (float *)malloc(nd * T * W * sizeof(float));
     for (size_t d = 0; d < nd; ++d)
@@ -404,16 +404,35 @@ void gno_fbp_ctf_f(const float *proj, size_t T, size_t H, size_t W, const float 
     cfg.min_defocus = D > 1 ? min_defocus : 0.0f;
     cfg.max_defocus = D > 1 ? max_defocus : 0.0f;
     cfg.angles = angles;
-    gno_recon_f(&cfg, sino, vol + y * Z * W);
+    gno_recon_f(&cfg, sino, out + (size_t)i * Z * W);
     free(sino);
   }
   free(corr);
 }
 
-void gno_fbp_ctf_d(const float *proj, size_t T, size_t H, size_t W, const float *angles,
+static size_t *row_range(size_t y_begin, size_t y_end) {
+  size_t n = y_end > y_begin ? y_end - y_begin : 0;
+  size_t *rows = (size_t *)malloc((n ? n : 1) * sizeof(size_t));
+  for (size_t i = 0; i < n; ++i) rows[i] = y_begin + i;
+  return rows;
+}
+
+void gno_fbp_ctf_f(const float *proj, size_t T, size_t H, size_t W, const float *angles,
                    const float *centre, float pixel_size, const float *ctf, size_t D,
                    float min_defocus, float max_defocus, const double *weights, int minus,
-                   size_t Z, double *vol, size_t y_begin, size_t y_end, int nthreads) {
+                   size_t Z, float *vol, size_t y_begin, size_t y_end, size_t t_begin,
+                   size_t t_end, int nthreads) {
+  size_t *rows = row_range(y_begin, y_end);
+  gno_fbp_ctf_rows_f(proj, T, H, W, angles, centre, pixel_size, ctf, D, min_defocus,
+                     max_defocus, weights, minus, Z, rows, y_end > y_begin ? y_end - y_begin : 0,
+                     vol + y_begin * Z * W, t_begin, t_end, nthreads);
+  free(rows);
+}
+
+void gno_fbp_ctf_rows_d(const float *proj, size_t T, size_t H, size_t W, const float *angles,
+                        const float *centre, float pixel_size, const float *ctf, size_t D,
+                        float min_defocus, float max_defocus, const double *weights, int minus,
+                        size_t Z, const size_t *rows, size_t nrows, double *out, int nthreads) {
   set_threads(nthreads);
   size_t nd = D > 0 ? D : 1;
   size_t img = H * W;
@@ -430,8 +449,8 @@ void gno_fbp_ctf_d(const float *proj, size_t T, size_t H, size_t W, const float 
     for (size_t k = 0; k < T * img; ++k) stack[k] = (double)proj[k];
   }
 #pragma omp parallel for schedule(dynamic, 1)
-  for (long yy = (long)y_begin; yy < (long)y_end; ++yy) {
-    size_t y = (size_t)yy;
+  for (long i = 0; i < (long)nrows; ++i) {
+    size_t y = rows[i];
     double *sino = (double *)malloc(nd * T * W * sizeof(double));
     for (size_t d = 0; d < nd; ++d)
       for (size_t t = 0; t < T; ++t) {
@@ -451,8 +470,19 @@ void gno_fbp_ctf_d(const float *proj, size_t T, size_t H, size_t W, const float 
     cfg.min_defocus = D > 1 ? min_defocus : 0.0f;
     cfg.max_defocus = D > 1 ? max_defocus : 0.0f;
     cfg.angles = angles;
-    gno_recon_d(&cfg, sino, vol + y * Z * W);
+    gno_recon_d(&cfg, sino, out + (size_t)i * Z * W);
     free(sino);
   }
   free(stack);
+}
+
+void gno_fbp_ctf_d(const float *proj, size_t T, size_t H, size_t W, const float *angles,
+                   const float *centre, float pixel_size, const float *ctf, size_t D,
+                   float min_defocus, float max_defocus, const double *weights, int minus,
+                   size_t Z, double *vol, size_t y_begin, size_t y_end, int nthreads) {
+  size_t *rows = row_range(y_begin, y_end);
+  gno_fbp_ctf_rows_d(proj, T, H, W, angles, centre, pixel_size, ctf, D, min_defocus,
+                     max_defocus, weights, minus, Z, rows, y_end > y_begin ? y_end - y_begin : 0,
+                     vol + y_begin * Z * W, nthreads);
+  free(rows);
 }

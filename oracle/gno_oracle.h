@@ -107,6 +107,18 @@ void gno_fbp_ctf_d(const float *proj, size_t T, size_t H, size_t W, const float 
                    const float *centre, float pixel_size, const float *ctf, size_t D,
                    float min_defocus, float max_defocus, const double *weights, int minus,
                    size_t Z, double *vol, size_t y_begin, size_t y_end, int nthreads);
+/* The same for an arbitrary list of rows: rows[i] (i < nrows) is written to
+ * out + i * Z * W, so a sample of bands of a large volume needs one
+ * correction pass and only the sampled rows' memory. */
+void gno_fbp_ctf_rows_f(const float *proj, size_t T, size_t H, size_t W, const float *angles,
+                        const float *centre, float pixel_size, const float *ctf, size_t D,
+                        float min_defocus, float max_defocus, const double *weights, int minus,
+                        size_t Z, const size_t *rows, size_t nrows, float *out, size_t t_begin,
+                        size_t t_end, int nthreads);
+void gno_fbp_ctf_rows_d(const float *proj, size_t T, size_t H, size_t W, const float *angles,
+                        const float *centre, float pixel_size, const float *ctf, size_t D,
+                        float min_defocus, float max_defocus, const double *weights, int minus,
+                        size_t Z, const size_t *rows, size_t nrows, double *out, int nthreads);
 
 #ifdef __cplusplus
 }

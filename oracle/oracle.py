@@ -88,6 +88,13 @@ def lib():
         L.gno_fbp_ctf_d.argtypes = [_f32p, _sz, _sz, _sz, _f32p, _f32p, ctypes.c_float, vp, _sz,
                                     ctypes.c_float, ctypes.c_float, vp, ctypes.c_int, _sz, _f64p,
                                     _sz, _sz, ctypes.c_int]
+        _szp = np.ctypeslib.ndpointer(dtype=np.uintp, flags="C_CONTIGUOUS")
+        L.gno_fbp_ctf_rows_f.argtypes = [_f32p, _sz, _sz, _sz, _f32p, _f32p, ctypes.c_float, vp,
+                                         _sz, ctypes.c_float, ctypes.c_float, vp, ctypes.c_int,
+                                         _sz, _szp, _sz, _f32p, _sz, _sz, ctypes.c_int]
+        L.gno_fbp_ctf_rows_d.argtypes = [_f32p, _sz, _sz, _sz, _f32p, _f32p, ctypes.c_float, vp,
+                                         _sz, ctypes.c_float, ctypes.c_float, vp, ctypes.c_int,
+                                         _sz, _szp, _sz, _f64p, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -146,12 +153,22 @@ def ctf_stack(width, height, pixel_size, energy, min_defocus, num_defocus, step_
     """complex64 (D, H, W) stack: correct.py:116-214 (keV, mm and degrees in)."""
     out = np.zeros((num_defocus, height, width), dtype=np.complex64)
     l = electron_wavelength(energy * 1000)
-    for d in range(num_defocus):
+
+    def slab(d):  # the C grid runs without the GIL: slabs in parallel threads
         df = min_defocus + d * step_defocus
         out[d] = ctf_grid(width, height, pixel_size, simple=True, l=l, df=df,
                           Cs=spherical_aberration * 1e7, Ca=astigmatism,
                           Pa=astigmatism_angle * math.pi / 180,
                           phi=phase_shift * math.pi / 180)
+
+    if num_defocus > 1 and width * height >= (1 << 18):
+        from concurrent.futures import ThreadPoolExecutor
+
+        with ThreadPoolExecutor(max_workers=min(num_defocus, os.cpu_count() or 1)) as ex:
+            list(ex.map(slab, range(num_defocus)))
+    else:
+        for d in range(num_defocus):
+            slab(d)
     return out
 
 
@@ -280,3 +297,41 @@ def fbp_ctf(proj, angles, centre, pixel_size, ctf=None, min_defocus=0.0, max_def
                             float(min_defocus), float(max_defocus), wptr, int(bool(minus)), Z,
                             vol, y0, y1, int(nthreads))
     return vol
+
+
+def fbp_ctf_rows(proj, angles, centre, pixel_size, rows, ctf=None, min_defocus=0.0,
+                 max_defocus=0.0, weights=None, minus=False, Z=None, precision="f32",
+                 nthreads=0):
+    """:func:`fbp_ctf` for a list of Y rows only: returns (len(rows), Z, W), row
+    i of it the volume's row rows[i].  One correction pass serves every row,
+    and only the listed rows' memory is allocated (bands of a volume too large
+    to hold whole)."""
+    proj = np.ascontiguousarray(proj, dtype=np.float32)
+    T, H, W = proj.shape
+    Z = W if Z is None else Z
+    rows = np.ascontiguousarray(rows, dtype=np.uintp)
+    if rows.size and (rows.min() < 0 or rows.max() >= H):
+        raise ValueError("row out of range")
+    angles = np.ascontiguousarray(angles, dtype=np.float32)
+    centre = np.ascontiguousarray(np.broadcast_to(np.asarray(centre, np.float32), (H,)))
+    D = 0
+    cptr = None
+    if ctf is not None:
+        ctf = np.ascontiguousarray(ctf, dtype=np.complex64)
+        D = ctf.shape[0]
+        cptr = ctf.ctypes.data
+    wptr = None
+    if weights is not None:
+        weights = np.ascontiguousarray(weights, dtype=np.float64)
+        wptr = weights.ctypes.data
+    if precision == "f32":
+        out = np.zeros((rows.size, Z, W), dtype=np.float32)
+        lib().gno_fbp_ctf_rows_f(proj, T, H, W, angles, centre, float(pixel_size), cptr, D,
+                                 float(min_defocus), float(max_defocus), wptr, int(bool(minus)),
+                                 Z, rows, rows.size, out, 0, T, int(nthreads))
+    else:
+        out = np.zeros((rows.size, Z, W), dtype=np.float64)
+        lib().gno_fbp_ctf_rows_d(proj, T, H, W, angles, centre, float(pixel_size), cptr, D,
+                                 float(min_defocus), float(max_defocus), wptr, int(bool(minus)),
+                                 Z, rows, rows.size, out, int(nthreads))
+    return out

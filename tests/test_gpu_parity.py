@@ -289,6 +289,35 @@ def test_tilt_chunks_of_different_magnitude(torch, oracle, staging):
         assert rel_l2(vol, ref64) < FP16_TOL
 
 
+# The same chunk hand-over in the fast backprojector: on a 128-pixel detector
+# the tiles span few enough slabs for the fast kernel (4 slabs per tile with 3
+# slabs, 2 with 1 slab).  Tilts 128-255 and 256-299 are scaled by different
+# magnitudes, so the FP16 form changes its common exponent and rescales its
+# accumulators at both chunk boundaries.
+@pytest.mark.parametrize("staging", ["f32", "f16"])
+@pytest.mark.parametrize("D,variant", [(3, 4), (1, 2)])
+def test_fast_backprojector_tilt_chunks(torch, oracle, staging, D, variant):
+    T, H, W, Z = 300, 6, 128, 48
+    plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=T, H=H, W=W, Z=Z, D=D, staging=staging,
+                                                 seed=9)
+    assert plan.backprojector == variant
+    proj[128:256] *= 40.0
+    proj[256:] *= 1.0 / 30.0
+    vol = plan.execute_host(proj)
+    plan.check()
+    ref32 = _oracle_volume(oracle, proj, ang, c, ctf, mn, mx, Z, "f32")
+    ref64 = _oracle_volume(oracle, proj, ang, c, ctf, mn, mx, Z, "f64")
+    if staging == "f32":
+        assert rel_l2(vol, ref32) < FP32_TOL
+        assert rel_l2(vol, ref64) < FP32_TOL
+    else:
+        assert rel_l2(vol, ref64) < FP16_TOL
+    exact = torch.empty(plan.volume_shape, dtype=torch.float32, device="cuda")
+    plan.stage(dev(torch, proj))
+    plan.backproject(exact, exact=True)
+    assert rel_l2(vol, exact.cpu().numpy()) < (1e-5 if staging == "f32" else 5e-4)
+
+
 # The host-buffer entry point overlaps its copies with the kernels (tilt groups
 # in, row slabs out; with CTF correction it filters row slab by row slab); it
 # must give exactly the device entry point's volume.  Shapes: power-of-two and

@@ -106,3 +106,22 @@ def angular_weights(angles):
         w[idx[i]] = si / sw if sw != 0 else 1.0
     w /= mean
     return w
+
+
+def test_row_list_oracle_equals_row_range(oracle):
+    """fbp_ctf_rows (a list of rows, one correction pass) gives exactly the rows
+    fbp_ctf computes for a contiguous range, in both precisions."""
+    rng = np.random.default_rng(2)
+    T, H, W, Z = 7, 12, 40, 30
+    ang = np.deg2rad(np.linspace(-60, 60, T)).astype(np.float32)
+    proj = rng.standard_normal((T, H, W)).astype(np.float32)
+    c = np.full(H, W / 2, np.float32)
+    mn, mx, step, nd = oracle.defocus_steps(25000.0, 3, None, W, c, 1.0)
+    ctf = oracle.ctf_stack(W, H, 1.0, 300, mn, nd, step, 2.7)
+    rows = np.array([0, 5, 6, 11])
+    for prec in ("f32", "f64"):
+        full = oracle.fbp_ctf(proj, ang, c, 1.0, ctf, float(mn - 25000.0), float(mx - 25000.0),
+                              Z=Z, precision=prec)
+        part = oracle.fbp_ctf_rows(proj, ang, c, 1.0, rows, ctf, float(mn - 25000.0),
+                                   float(mx - 25000.0), Z=Z, precision=prec)
+        np.testing.assert_array_equal(part, full[rows])
