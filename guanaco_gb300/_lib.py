@@ -144,6 +144,7 @@ SIGNATURES = {
     "gnc_fbp_check": (c_int, [c_void, c_void]),
     "gnc_fbp_launches": (c_int, [c_void]),
     "gnc_fbp_backprojector": (c_int, [c_void]),
+    "gnc_fbp_live_slabs": (c_int, [c_void, c_void, c_void]),
     "gnc_debug_wait_probe": (c_int, [ctypes.c_uint]),
     "gnc_server_create": (c_int, [c_size, c_int, ctypes.POINTER(c_void)]),
     "gnc_server_destroy": (c_int, [c_void]),

@@ -181,6 +181,7 @@ struct gnc_fbp_plan {
   void *staged = nullptr;   // (Y2, D, T, W) pairs
   int8_t *row_exp = nullptr;
   int8_t *sign = nullptr;   // (D, H, W/2 + 1)
+  int2 *live = nullptr;     // (T): first and last slab the volume reads (CTF, D > 1)
   // everything that differs between two requests of the same shape, in one
   // block (ParamLayout): views into it
   unsigned char *params = nullptr;
@@ -214,6 +215,7 @@ static void plan_free(gnc_fbp_plan *p) {
   cudaFree(p->staged);
   cudaFree(p->row_exp);
   cudaFree(p->sign);
+  cudaFree(p->live);
   cudaFree(p->params);
   cudaFree(p->err);
   cudaFree(p->io_in);
@@ -346,7 +348,7 @@ size_t plan_bytes(const gnc_fbp_desc *d) {
     const size_t per_tilt = D * H * half * sizeof(float2);
     const size_t chunk = flip_chunk(T, per_tilt);
     b += T * H * half * sizeof(float2) + 2 * chunk * D * H * half * sizeof(float2) +
-         sign_table_bytes((int)D, (int)H, (int)W);
+         sign_table_bytes((int)D, (int)H, (int)W) + (D > 1 ? T * sizeof(int2) : 0);
   }
   b += (Y2 * D * T * W + 8) * kStagedPixelBytes;
   if (d->staging == GNC_STAGE_F16) b += Y2 * D * T * 2;
@@ -495,6 +497,7 @@ int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
       if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_rows[b], cudaEventDisableTiming);
     }
     if (e == cudaSuccess) e = dalloc(p, &p->sign, sign_table_bytes(p->D, p->H, p->W));
+    if (e == cudaSuccess && p->D > 1) e = dalloc(p, &p->live, (size_t)p->T);
   }
   // +8 pixels: a 16-byte aligned bulk copy of the last row may run past its end
   const size_t elems = (size_t)p->Y2 * p->D * p->T * p->W + 8;
@@ -547,7 +550,7 @@ static int flip_rows(gnc_fbp_plan *p, RowStageArgs r, int t_begin, int t_end, fl
     const int b = k & 1;
     float2 *g = p->gbuf + b * gsz;
     if (k >= 2) GNC_CUDA(cudaStreamWaitEvent(p->s_flip, p->ev_rows[b], 0));
-    GNC_CUDA(launch_column_flip(p->spec, g, p->sign, c0, nt, p->D, p->H, p->W, p->s_flip));
+    GNC_CUDA(launch_column_flip(p->spec, g, p->sign, c0, nt, p->D, p->H, p->W, r.live, p->s_flip));
     GNC_CUDA(cudaEventRecord(p->ev_flip[b], p->s_flip));
     GNC_CUDA(cudaStreamWaitEvent(s, p->ev_flip[b], 0));
     r.g = g;
@@ -578,9 +581,11 @@ int gnc_fbp_stage(gnc_fbp_plan *p, const float *d_input, void *stream) {
   if (p->correct) {
     GNC_CUDA(launch_sign_table(p->sargs, p->sign, s));
     GNC_CUDA(launch_sign_pack(p->sign, p->D, p->H, p->W, s));
+    if (p->live) GNC_CUDA(launch_live_slabs(bp_args(p, nullptr), p->live, s));
     GNC_CUDA(launch_rfft_rows(d_input, p->spec, p->T, p->H, p->W, s));
     GNC_CUDA(launch_column_fft(p->spec, p->T, p->H, p->W, s));
     r.input_spectra = 1;
+    r.live = p->live;  // only the (tilt, slab) pairs some voxel reads
     const int st = flip_rows(p, r, 0, p->T, nullptr, s);
     if (st != GNC_OK) return st;
   } else {
@@ -694,7 +699,9 @@ static int execute_host_pipelined(gnc_fbp_plan *p, const float *h_input, float *
   if (p->correct) {
     GNC_CUDA(launch_sign_table(p->sargs, p->sign, s));
     GNC_CUDA(launch_sign_pack(p->sign, p->D, p->H, p->W, s));
+    if (p->live) GNC_CUDA(launch_live_slabs(bp_args(p, nullptr), p->live, s));
     r.input_spectra = 1;
+    r.live = p->live;  // only the (tilt, slab) pairs some voxel reads
   } else {
     r.input_spectra = 0;
     r.rows = p->io_in;
@@ -710,7 +717,7 @@ static int execute_host_pipelined(gnc_fbp_plan *p, const float *h_input, float *
       GNC_CUDA(launch_column_fft(spec, n, p->H, p->W, s));
       if (slab_major) {
         GNC_CUDA(launch_column_flip(p->spec, p->gfull + (size_t)t0 * p->D * p->H * half, p->sign,
-                                    t0, n, p->D, p->H, p->W, s));
+                                    t0, n, p->D, p->H, p->W, p->live, s));
       } else {
         const int st = flip_rows(p, r, t0, t0 + n, nullptr, s);
         if (st != GNC_OK) return st;
@@ -829,8 +836,22 @@ int gnc_fbp_launches(const gnc_fbp_plan *p) {
   if (!p) return 0;
   if (!p->correct) return 2;  // row stage, backprojection
   const int chunks = (p->T + p->chunk - 1) / p->chunk;
-  // sign table (+ its packed copy), row and column transforms, per chunk flip + rows, BP
-  return 3 + (sign_pack_used(p->H) ? 1 : 0) + 2 * chunks + 1;
+  // sign table (+ its packed copy, + the live slab ranges), row and column
+  // transforms, per chunk flip + rows, BP
+  return 3 + (sign_pack_used(p->H) ? 1 : 0) + (p->live ? 1 : 0) + 2 * chunks + 1;
+}
+
+int gnc_fbp_live_slabs(gnc_fbp_plan *p, int32_t *h_out, void *stream) {
+  GNC_REQUIRE(p != nullptr && h_out != nullptr);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!p->live) {  // one slab, or no correction: every tilt reads slab 0 only
+    for (int t = 0; t < p->T; ++t) h_out[2 * t] = h_out[2 * t + 1] = 0;
+    return GNC_OK;
+  }
+  GNC_CUDA(launch_live_slabs(bp_args(p, nullptr), p->live, s));
+  GNC_CUDA(cudaMemcpyAsync(h_out, p->live, (size_t)p->T * sizeof(int2), cudaMemcpyDeviceToHost, s));
+  GNC_CUDA(cudaStreamSynchronize(s));
+  return GNC_OK;
 }
 
 int gnc_fbp_backprojector(const gnc_fbp_plan *p) {
@@ -1047,7 +1068,7 @@ int gnc_correct(const float *image, const float *ctf, float *rec, size_t xsize, 
   if (e == cudaSuccess) e = launch_sign_pack(sign, D, H, W, s);
   if (e == cudaSuccess) e = launch_rfft_rows(dimg, spec, 1, H, W, s);
   if (e == cudaSuccess) e = launch_column_fft(spec, 1, H, W, s);
-  if (e == cudaSuccess) e = launch_column_flip(spec, g, sign, 0, 1, D, H, W, s);
+  if (e == cudaSuccess) e = launch_column_flip(spec, g, sign, 0, 1, D, H, W, nullptr, s);
   if (e == cudaSuccess) {
     RowStageArgs r{};
     r.input_spectra = 1;

@@ -43,7 +43,8 @@ __global__ void __launch_bounds__(256 * C, 4 / C) k_column_b4096(const float2 *_
                                                              float2 *__restrict__ dst,
                                                              const unsigned long long *__restrict__ sign,
                                                              int t0, int D, int W,
-                                                             const float2 *__restrict__ roots) {
+                                                             const float2 *__restrict__ roots,
+                                                             const int2 *__restrict__ live) {
   extern __shared__ float2 smem_cb[];
   const int c = threadIdx.x % C, l = threadIdx.x / C;
   const int half = W / 2;
@@ -51,6 +52,7 @@ __global__ void __launch_bounds__(256 * C, 4 / C) k_column_b4096(const float2 *_
   const int d = FLIP ? blockIdx.y : 0;
   const int tl = blockIdx.z;
   const int t = t0 + tl;
+  if (FLIP && !slab_live(live, t, d)) return;  // no voxel reads this (tilt, slab)
   const float2 *F = src + (size_t)t * kN * half;
   const int sw = half + 1;
   // the 16 signs of rows l + 256 m: one packed entry (d, l, kx)
@@ -109,6 +111,7 @@ __global__ void __launch_bounds__(256, 2) k_row_b4096(RowStageArgs a,
   const int rem = (int)(pair - (long)tl * a.D * Y2);
   const int d = rem / Y2, y2 = a.y2_begin + (rem - d * Y2);
   const int t = a.t0 + tl;
+  if (!slab_live(a.live, t, d)) return;  // no voxel reads this (tilt, slab): whole block
   const int ya = 2 * y2;
   const bool hb = ya + 1 < a.H;
   constexpr int half = kN / 2;
@@ -240,7 +243,7 @@ __global__ void __launch_bounds__(256, 2) k_row_b4096(RowStageArgs a,
 // ---------------------------------------------------------------- launchers
 template <bool FLIP>
 static cudaError_t column_b4096(const float2 *src, float2 *dst, const int8_t *sign, int t0,
-                                int nt, int D, int W, cudaStream_t s) {
+                                int nt, int D, int W, const int2 *live, cudaStream_t s) {
   FftPlan p;
   if (!make_fft_plan(kN, &p)) return cudaErrorInvalidValue;
   constexpr int C = kColC;
@@ -250,17 +253,17 @@ static cudaError_t column_b4096(const float2 *src, float2 *dst, const int8_t *si
   dim3 grid((half + C - 1) / C, FLIP ? D : 1, nt);
   const unsigned long long *packed = FLIP ? sign_packed(sign, D, kN, W) : nullptr;
   if (((uintptr_t)packed & 7) != 0) return cudaErrorMisalignedAddress;  // 8-byte loads
-  k_column_b4096<FLIP, C><<<grid, 256 * C, smem, s>>>(src, dst, packed, t0, D, W, p.roots);
+  k_column_b4096<FLIP, C><<<grid, 256 * C, smem, s>>>(src, dst, packed, t0, D, W, p.roots, live);
   return cudaGetLastError();
 }
 
 cudaError_t launch_column_fft_b4096(float2 *spec, int T, int W, cudaStream_t s) {
-  return column_b4096<false>(spec, spec, nullptr, 0, T, 1, W, s);
+  return column_b4096<false>(spec, spec, nullptr, 0, T, 1, W, nullptr, s);
 }
 
 cudaError_t launch_column_flip_b4096(const float2 *spec, float2 *g, const int8_t *sign, int t0,
-                                     int nt, int D, int W, cudaStream_t s) {
-  return column_b4096<true>(spec, g, sign, t0, nt, D, W, s);
+                                     int nt, int D, int W, const int2 *live, cudaStream_t s) {
+  return column_b4096<true>(spec, g, sign, t0, nt, D, W, live, s);
 }
 
 template <bool SPECTRA, bool RAMP, bool STAGED, bool F16>

@@ -104,6 +104,35 @@ __global__ void k_slab_map(BpArgs a, int32_t *__restrict__ out) {
   out[((size_t)t * a.Z + z) * a.X + x] = k;
 }
 
+// One thread per tilt: the slab index at the volume's four corners (the index
+// is monotone in x and in z) gives the slabs any voxel reads.
+__global__ void k_live_slabs(BpArgs a, int2 *__restrict__ live) {
+  if (a.dyn) {
+    a.dscale = a.dyn[0];
+    a.doffset = a.dyn[1];
+  }
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= a.T) return;
+  int lo = 0, hi = 0;
+  if (a.D > 1) {
+    const TiltGeom g = a.geom[t];
+    const float x0 = voxel_coord(0, a.X), x1 = voxel_coord(a.X - 1, a.X);
+    const float z0 = voxel_coord(0, a.Z), z1 = voxel_coord(a.Z - 1, a.Z);
+    const int k00 = slab_index(x0, z0, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
+    const int k01 = slab_index(x0, z1, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
+    const int k10 = slab_index(x1, z0, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
+    const int k11 = slab_index(x1, z1, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
+    lo = min(min(k00, k01), min(k10, k11));
+    hi = max(max(k00, k01), max(k10, k11));
+  }
+  live[t] = make_int2(lo, hi);
+}
+
+cudaError_t launch_live_slabs(const BpArgs &a, int2 *live, cudaStream_t s) {
+  k_live_slabs<<<(a.T + 127) / 128, 128, 0, s>>>(a, live);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_slab_map(const BpArgs &a, int32_t *out, cudaStream_t s) {
   dim3 block(32, 8);
   dim3 grid((a.X + 31) / 32, (a.Z + 7) / 8, a.T);

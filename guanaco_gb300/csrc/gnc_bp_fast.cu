@@ -230,6 +230,11 @@ k_bp_fast(BpArgs a) {
   for (int j = 0; j < B; ++j) zf[j] = voxel_coordf(z0 + wz * 8 * B + 8 * j + lz, a.Z);
   const float cx0 = voxel_coordf(x0, a.X), cx1 = voxel_coordf(x0 + P::TX - 1, a.X);
   const float cz0 = voxel_coordf(z0, a.Z), cz1 = voxel_coordf(z0 + P::TZ - 1, a.Z);
+  // the tile's corners inside the volume: the slabs its stored voxels read
+  // (voxels past the volume's edge read slots of these slabs and are not
+  // stored; the flip and row stage skip slabs no stored voxel reads)
+  const float vx1 = voxel_coordf(min(x0 + P::TX, a.X) - 1, a.X);
+  const float vz1 = voxel_coordf(min(z0 + P::TZ, a.Z) - 1, a.Z);
 
   if (tid == 0) {
     // every lane of warp 0 arrives once per phase (with its own byte count)
@@ -307,9 +312,9 @@ k_bp_fast(BpArgs a) {
       int k_lo = 0, k_hi = 0;
       if (a.D > 1) {
         const int k00 = slab_index(cx0, cz0, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
-        const int k01 = slab_index(cx0, cz1, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
-        const int k10 = slab_index(cx1, cz0, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
-        const int k11 = slab_index(cx1, cz1, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
+        const int k01 = slab_index(cx0, vz1, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
+        const int k10 = slab_index(vx1, cz0, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
+        const int k11 = slab_index(vx1, vz1, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
         k_lo = min(min(k00, k01), min(k10, k11));
         k_hi = max(max(k00, k01), max(k10, k11));
       }

@@ -80,8 +80,16 @@ cudaError_t launch_sign_pack(int8_t *sign, int D, int H, int W, cudaStream_t s);
 __device__ __forceinline__ int packed_sign(unsigned long long w, int m) {
   return (int)((w >> (3 * m)) & 7ull) - 2;
 }
+// live: per tilt, the first and last slab any voxel of the volume reads (the
+// flip and the row stage skip the other (tilt, slab) pairs), or null: all.
 cudaError_t launch_column_flip(const float2 *spec, float2 *g, const int8_t *sign, int t0, int nt,
-                               int D, int H, int W, cudaStream_t s);
+                               int D, int H, int W, const int2 *live, cudaStream_t s);
+// Whether slab d of tilt t is read by any voxel (live as above).
+__device__ __forceinline__ bool slab_live(const int2 *live, int t, int d) {
+  if (!live) return true;
+  const int2 r = live[t];
+  return d >= r.x && d <= r.y;
+}
 
 // The 2 * symmetrised phase-flip sign for every (slab, ky, kx <= W/2), from the
 // FP64 CTF phase (include/guanaco/ctf.h:88-101, 233-273; correct.h:30-39).
@@ -128,6 +136,8 @@ struct RowStageArgs {
   void *staged;          // float2 pairs or FP16 records
   int8_t *row_exp;       // (Y2, D, T, 2) FP16 exponents when staging == F16
   float *out_rows;       // plain rows: (nt, D, H, N) at [t][d][y][n]
+  const int2 *live;      // per tilt (first, last) slab the volume reads; others are
+                         // skipped (staged output only), or null: all slabs
 };
 cudaError_t launch_row_stage(const RowStageArgs &a, cudaStream_t s);
 
@@ -172,6 +182,10 @@ int backproject_fast_variant(const BpArgs &a);
 cudaError_t launch_backproject_exact(const BpArgs &a, cudaStream_t s);
 cudaError_t launch_backproject_fast(const BpArgs &a, cudaStream_t s);
 cudaError_t launch_slab_map(const BpArgs &a, int32_t *out, cudaStream_t s);
+// Per tilt, the first and last slab any voxel of the (Z, X) volume reads:
+// the slab index is monotone in x and in z, so the extremes lie at the
+// volume's corners (the same float expression as the backprojectors).
+cudaError_t launch_live_slabs(const BpArgs &a, int2 *live, cudaStream_t s);
 
 // Single-slice backprojection of plain filtered rows (D, T, N) into (Z, X):
 // the per-call path of guanaco.detail.recon.
@@ -192,7 +206,7 @@ cudaError_t launch_rfft_rows_p2(const float *proj, float2 *spec, int T, int H, i
                                 cudaStream_t s);
 cudaError_t launch_column_fft_p2(float2 *spec, int T, int H, int W, cudaStream_t s);
 cudaError_t launch_column_flip_p2(const float2 *spec, float2 *g, const int8_t *sign, int t0,
-                                  int nt, int D, int H, int W, cudaStream_t s);
+                                  int nt, int D, int H, int W, const int2 *live, cudaStream_t s);
 cudaError_t launch_row_stage_p2(const RowStageArgs &a, cudaStream_t s);
 
 // One-warp register FFT kernels for 1024-point rows / columns
@@ -200,19 +214,20 @@ cudaError_t launch_row_stage_p2(const RowStageArgs &a, cudaStream_t s);
 cudaError_t launch_rfft_rows_w1024(const float *proj, float2 *spec, int T, int H, cudaStream_t s);
 cudaError_t launch_column_fft_w1024(float2 *spec, int T, int W, cudaStream_t s);
 cudaError_t launch_column_flip_w1024(const float2 *spec, float2 *g, const int8_t *sign, int t0,
-                                     int nt, int D, int W, cudaStream_t s);
+                                     int nt, int D, int W, const int2 *live, cudaStream_t s);
 cudaError_t launch_row_stage_w1024(const RowStageArgs &a, cudaStream_t s);
 // Register-transform kernels for 128-, 256-, 384- and 512-pixel columns and rows
 // (gnc_w512_kernels.cu); the launchers above prefer them for those sizes.
 cudaError_t launch_column_fft_w512(float2 *spec, int T, int H, int W, cudaStream_t s);
 cudaError_t launch_column_flip_w512(const float2 *spec, float2 *g, const int8_t *sign, int t0,
-                                    int nt, int D, int H, int W, cudaStream_t s);
+                                    int nt, int D, int H, int W, const int2 *live,
+                                    cudaStream_t s);
 cudaError_t launch_row_stage_w512(const RowStageArgs &a, cudaStream_t s);
 // Block-transform kernels for 4096-pixel columns and rows
 // (gnc_b4096_kernels.cu); the launchers above prefer them for that size.
 cudaError_t launch_column_fft_b4096(float2 *spec, int T, int W, cudaStream_t s);
 cudaError_t launch_column_flip_b4096(const float2 *spec, float2 *g, const int8_t *sign, int t0,
-                                     int nt, int D, int W, cudaStream_t s);
+                                     int nt, int D, int W, const int2 *live, cudaStream_t s);
 cudaError_t launch_row_stage_b4096(const RowStageArgs &a, cudaStream_t s);
 
 // Exact slab index of the reference (reconstructor.cpp:66-72): the height and

@@ -140,12 +140,13 @@ cudaError_t launch_column_fft(float2 *spec, int T, int H, int W, cudaStream_t s)
 // (column tile, slab, tilt of the chunk).
 __global__ void k_column_flip(const float2 *__restrict__ spec, float2 *__restrict__ g,
                               const int8_t *__restrict__ sign, int t0, int D, int H, int W, int C,
-                              FftPlan plan) {
+                              FftPlan plan, const int2 *__restrict__ live) {
   extern __shared__ float2 smem[];
   const int half = W / 2;
   const int d = blockIdx.y;
   const int tl = blockIdx.z;
   const int t = t0 + tl;
+  if (!slab_live(live, t, d)) return;  // no voxel reads this (tilt, slab)
   const int c0 = blockIdx.x * C;
   float2 *b0 = smem, *b1 = smem + H * C;
   const float2 *F = spec + (size_t)t * H * half;
@@ -180,11 +181,12 @@ __global__ void k_column_flip(const float2 *__restrict__ spec, float2 *__restric
 }
 
 cudaError_t launch_column_flip(const float2 *spec, float2 *g, const int8_t *sign, int t0, int nt,
-                               int D, int H, int W, cudaStream_t s) {
-  if (H == 1024) return launch_column_flip_w1024(spec, g, sign, t0, nt, D, W, s);
-  if (H == 4096) return launch_column_flip_b4096(spec, g, sign, t0, nt, D, W, s);
-  if (H == 128 || H == 256 || H == 384 || H == 512) return launch_column_flip_w512(spec, g, sign, t0, nt, D, H, W, s);
-  if (pow2_fast(H)) return launch_column_flip_p2(spec, g, sign, t0, nt, D, H, W, s);
+                               int D, int H, int W, const int2 *live, cudaStream_t s) {
+  if (H == 1024) return launch_column_flip_w1024(spec, g, sign, t0, nt, D, W, live, s);
+  if (H == 4096) return launch_column_flip_b4096(spec, g, sign, t0, nt, D, W, live, s);
+  if (H == 128 || H == 256 || H == 384 || H == 512)
+    return launch_column_flip_w512(spec, g, sign, t0, nt, D, H, W, live, s);
+  if (pow2_fast(H)) return launch_column_flip_p2(spec, g, sign, t0, nt, D, H, W, live, s);
   FftPlan plan;
   if (!make_fft_plan(H, &plan)) return cudaErrorInvalidValue;
   const int half = W / 2;
@@ -193,7 +195,7 @@ cudaError_t launch_column_flip(const float2 *spec, float2 *g, const int8_t *sign
   size_t smem = 2ull * H * C * sizeof(float2);
   if (cudaError_t e_attr = ensure_dynamic_smem<k_column_flip>(200 * 1024)) return e_attr;
   dim3 grid((half + C - 1) / C, D, nt);
-  k_column_flip<<<grid, 256, smem, s>>>(spec, g, sign, t0, D, H, W, C, plan);
+  k_column_flip<<<grid, 256, smem, s>>>(spec, g, sign, t0, D, H, W, C, plan, live);
   return cudaGetLastError();
 }
 

@@ -109,7 +109,7 @@ struct ColTile {
 template <int H, bool FLIP>
 __global__ void __launch_bounds__(ColTile<H>::THREADS) k_column_p2(
     const float2 *__restrict__ src, float2 *__restrict__ dst, const int8_t *__restrict__ sign,
-    int t0, int D, int W, const float2 *__restrict__ roots) {
+    int t0, int D, int W, const float2 *__restrict__ roots, const int2 *__restrict__ live) {
   using P = Pow2<H>;
   constexpr int C = ColTile<H>::C;
   constexpr int NTH = ColTile<H>::THREADS;
@@ -121,6 +121,7 @@ __global__ void __launch_bounds__(ColTile<H>::THREADS) k_column_p2(
   const int d = FLIP ? blockIdx.y : 0;
   const int tl = blockIdx.z;
   const int t = t0 + tl;
+  if (FLIP && !slab_live(live, t, d)) return;  // no voxel reads this (tilt, slab)
   const float2 *F = src + (size_t)t * H * half;
   const int sw = half + 1;
   const int8_t *sg = FLIP ? sign + (size_t)d * H * sw : nullptr;
@@ -173,12 +174,16 @@ __global__ void __launch_bounds__(256) k_row_p2(RowStageArgs a, const float2 *__
   const int Y2 = row_pairs(a);  // row pairs of this launch
   const long npairs = (long)a.nt * a.D * Y2;
   long pair = (long)blockIdx.x * GPB + g;
-  const bool active = pair < npairs;
+  bool active = pair < npairs;
   if (!active) pair = npairs - 1;
   const int tl = (int)(pair / ((long)a.D * Y2));
   const int rem = (int)(pair - (long)tl * a.D * Y2);
   const int d = rem / Y2, y2 = a.y2_begin + (rem - d * Y2);
   const int t = a.t0 + tl;
+  // a (tilt, slab) no voxel reads is not stored; a block with none to store
+  // returns before its first barrier
+  active = active && slab_live(a.live, t, d);
+  if (!__syncthreads_or(active)) return;
   const int ya = 2 * y2;
   const bool hb = ya + 1 < a.H;
   constexpr int half = N / 2;
@@ -372,28 +377,29 @@ cudaError_t launch_rfft_rows_p2(const float *proj, float2 *spec, int T, int H, i
 
 template <int H, bool FLIP>
 static cudaError_t column_p2(const float2 *src, float2 *dst, const int8_t *sign, int t0, int nt,
-                             int D, int W, cudaStream_t s) {
+                             int D, int W, const int2 *live, cudaStream_t s) {
   FftPlan p;
   if (!make_fft_plan(H, &p)) return cudaErrorInvalidValue;
   using CT = ColTile<H>;
   if (cudaError_t e_attr = ensure_dynamic_smem<k_column_p2<H, FLIP>>((int)CT::SMEM)) return e_attr;
   const int half = W / 2;
   dim3 grid((half + CT::C - 1) / CT::C, FLIP ? D : 1, nt);
-  k_column_p2<H, FLIP><<<grid, CT::THREADS, CT::SMEM, s>>>(src, dst, sign, t0, D, W, p.roots);
+  k_column_p2<H, FLIP><<<grid, CT::THREADS, CT::SMEM, s>>>(src, dst, sign, t0, D, W, p.roots,
+                                                            live);
   return cudaGetLastError();
 }
 
 cudaError_t launch_column_fft_p2(float2 *spec, int T, int H, int W, cudaStream_t s) {
   switch (H) {
-    case 2048: return column_p2<2048, false>(spec, spec, nullptr, 0, T, 1, W, s);
+    case 2048: return column_p2<2048, false>(spec, spec, nullptr, 0, T, 1, W, nullptr, s);
   }
   return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_column_flip_p2(const float2 *spec, float2 *g, const int8_t *sign, int t0,
-                                  int nt, int D, int H, int W, cudaStream_t s) {
+                                  int nt, int D, int H, int W, const int2 *live, cudaStream_t s) {
   switch (H) {
-    case 2048: return column_p2<2048, true>(spec, g, sign, t0, nt, D, W, s);
+    case 2048: return column_p2<2048, true>(spec, g, sign, t0, nt, D, W, live, s);
   }
   return cudaErrorInvalidValue;
 }

@@ -37,6 +37,10 @@ __global__ void k_row_stage(RowStageArgs a, FftPlan planN, FftPlan plan2N, int r
       int rem = (int)(P - (long)tl * a.D * Y2);
       int d = rem / Y2, y2 = a.y2_begin + (rem - d * Y2);
       int ya = 2 * y2;
+      if (!slab_live(a.live, a.t0 + tl, d)) {  // no voxel reads it: zeros, not stored
+        bufa[s * L + k] = z;
+        continue;
+      }
       bool hb = ya + 1 < a.H;
       if (SPECTRA) {
         const int half = N / 2;
@@ -104,6 +108,7 @@ __global__ void k_row_stage(RowStageArgs a, FftPlan planN, FftPlan plan2N, int r
     int t = a.t0 + tl;
     int ya = 2 * y2;
     bool hb = ya + 1 < a.H;
+    if (!slab_live(a.live, t, d)) continue;  // the same for every thread of the block
     float f = a.tilt_factor ? a.tilt_factor[t] : 1.0f;
     const float2 *row = cur + s * L;
     if (STAGED && !F16) {

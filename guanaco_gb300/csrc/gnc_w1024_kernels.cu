@@ -78,8 +78,13 @@ __global__ void __launch_bounds__(256, 2) k_column_w1024(const float2 *__restric
                                                       float2 *__restrict__ dst,
                                                       const ulonglong2 *__restrict__ sign,
                                                       int t0, int D, int W,
-                                                      const float2 *__restrict__ roots) {
+                                                      const float2 *__restrict__ roots,
+                                                      const int2 *__restrict__ live) {
   constexpr int C = 8, P = 9;
+  const int d = FLIP ? blockIdx.y : 0;
+  const int tl = blockIdx.z;
+  const int t = t0 + tl;
+  if (FLIP && !slab_live(live, t, d)) return;  // no voxel reads this (tilt, slab)
   extern __shared__ float2 smem_w[];
   float2 *tw = smem_w;
   float2 *tile = smem_w + 1024;
@@ -87,9 +92,6 @@ __global__ void __launch_bounds__(256, 2) k_column_w1024(const float2 *__restric
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int half = W / 2;
   const int c0 = blockIdx.x * C;
-  const int d = FLIP ? blockIdx.y : 0;
-  const int tl = blockIdx.z;
-  const int t = t0 + tl;
   const float2 *F = src + (size_t)t * kN * half;
   const int sw = half + 1;
   // each thread moves one column (c) of rows y0 + 32 j: all 32 loads in flight;
@@ -178,6 +180,7 @@ __global__ void __launch_bounds__(128, 3) k_row_w1024(RowStageArgs a,
   const int rem = (int)(pair - (long)tl * a.D * Y2);
   const int d = rem / Y2, y2 = a.y2_begin + (rem - d * Y2);
   const int t = a.t0 + tl;
+  if (!slab_live(a.live, t, d)) return;  // no voxel reads this (tilt, slab)
   const int ya = 2 * y2;
   const bool hb = ya + 1 < a.H;
   constexpr int half = kN / 2;
@@ -360,7 +363,7 @@ cudaError_t launch_rfft_rows_w1024(const float *proj, float2 *spec, int T, int H
 
 template <bool FLIP>
 static cudaError_t column_w1024(const float2 *src, float2 *dst, const int8_t *sign, int t0,
-                                int nt, int D, int W, cudaStream_t s) {
+                                int nt, int D, int W, const int2 *live, cudaStream_t s) {
   const float2 *roots;
   if (!roots_for(kN, &roots)) return cudaErrorInvalidValue;
   const size_t smem = (1024 + (size_t)kWarpFftSlots * 9) * sizeof(float2);
@@ -369,17 +372,17 @@ static cudaError_t column_w1024(const float2 *src, float2 *dst, const int8_t *si
   const ulonglong2 *packed = FLIP ? (const ulonglong2 *)sign_packed(sign, D, kN, W) : nullptr;
   if (((uintptr_t)packed & 15) != 0) return cudaErrorMisalignedAddress;  // 16-byte loads
   dim3 grid((half + 7) / 8, FLIP ? D : 1, nt);
-  k_column_w1024<FLIP><<<grid, 256, smem, s>>>(src, dst, packed, t0, D, W, roots);
+  k_column_w1024<FLIP><<<grid, 256, smem, s>>>(src, dst, packed, t0, D, W, roots, live);
   return cudaGetLastError();
 }
 
 cudaError_t launch_column_fft_w1024(float2 *spec, int T, int W, cudaStream_t s) {
-  return column_w1024<false>(spec, spec, nullptr, 0, T, 1, W, s);
+  return column_w1024<false>(spec, spec, nullptr, 0, T, 1, W, nullptr, s);
 }
 
 cudaError_t launch_column_flip_w1024(const float2 *spec, float2 *g, const int8_t *sign, int t0,
-                                     int nt, int D, int W, cudaStream_t s) {
-  return column_w1024<true>(spec, g, sign, t0, nt, D, W, s);
+                                     int nt, int D, int W, const int2 *live, cudaStream_t s) {
+  return column_w1024<true>(spec, g, sign, t0, nt, D, W, live, s);
 }
 
 template <bool SPECTRA, bool RAMP, bool STAGED, bool F16>

@@ -54,7 +54,8 @@ __global__ void __launch_bounds__(256, 3) k_column_w512(const float2 *__restrict
                                                        float2 *__restrict__ dst,
                                                        const unsigned long long *__restrict__ sign,
                                                        int t0, int D, int W,
-                                                       const float2 *__restrict__ roots) {
+                                                       const float2 *__restrict__ roots,
+                                                       const int2 *__restrict__ live) {
   using P = ColW512<H>;
   constexpr int C = P::C, L = WarpFftShape<H>::L;
   extern __shared__ float2 smem_c5[];
@@ -64,6 +65,7 @@ __global__ void __launch_bounds__(256, 3) k_column_w512(const float2 *__restrict
   const int d = FLIP ? blockIdx.y : 0;
   const int tl = blockIdx.z;
   const int t = t0 + tl;
+  if (FLIP && !slab_live(live, t, d)) return;  // no voxel reads this (tilt, slab)
   const float2 *F = src + (size_t)t * H * half;
   const int sw = half + 1;
   const int c = threadIdx.x % C, r0 = threadIdx.x / C;
@@ -151,12 +153,16 @@ __global__ void __launch_bounds__(128) k_row_w512(RowStageArgs a, const float2 *
   const int Y2 = row_pairs(a);  // row pairs of this launch
   const long npairs = (long)a.nt * a.D * Y2;
   long pair = (long)blockIdx.x * PPB + w * TPW + sub;
-  const bool active = act && pair < npairs;
+  bool active = act && pair < npairs;
   if (pair >= npairs) pair = npairs - 1;  // the lanes of a warp stay together for its shuffles
   const int tl = (int)(pair / ((long)a.D * Y2));
   const int rem = (int)(pair - (long)tl * a.D * Y2);
   const int d = rem / Y2, y2 = a.y2_begin + (rem - d * Y2);
   const int t = a.t0 + tl;
+  // a (tilt, slab) no voxel reads is not stored; a warp with none to store
+  // returns (no block barrier follows)
+  active = active && slab_live(a.live, t, d);
+  if (!__any_sync(0xffffffffu, active)) return;
   const int ya = 2 * y2;
   const bool hb = ya + 1 < a.H;
   constexpr int half = N / 2;
@@ -288,7 +294,7 @@ __global__ void __launch_bounds__(128) k_row_w512(RowStageArgs a, const float2 *
 // ---------------------------------------------------------------- launchers
 template <int H, bool FLIP>
 static cudaError_t column_w512(const float2 *src, float2 *dst, const int8_t *sign, int t0, int nt,
-                               int D, int W, cudaStream_t s) {
+                               int D, int W, const int2 *live, cudaStream_t s) {
   using P = ColW512<H>;
   FftPlan p;
   if (!make_fft_plan(H, &p)) return cudaErrorInvalidValue;
@@ -297,27 +303,28 @@ static cudaError_t column_w512(const float2 *src, float2 *dst, const int8_t *sig
   if (((uintptr_t)packed & 7) != 0) return cudaErrorMisalignedAddress;  // 8-byte loads
   const int half = W / 2;
   dim3 grid((half + P::C - 1) / P::C, FLIP ? D : 1, nt);
-  k_column_w512<H, FLIP><<<grid, 256, P::SMEM, s>>>(src, dst, packed, t0, D, W, p.roots);
+  k_column_w512<H, FLIP><<<grid, 256, P::SMEM, s>>>(src, dst, packed, t0, D, W, p.roots, live);
   return cudaGetLastError();
 }
 
 cudaError_t launch_column_fft_w512(float2 *spec, int T, int H, int W, cudaStream_t s) {
   switch (H) {
-    case 128: return column_w512<128, false>(spec, spec, nullptr, 0, T, 1, W, s);
-    case 256: return column_w512<256, false>(spec, spec, nullptr, 0, T, 1, W, s);
-    case 384: return column_w512<384, false>(spec, spec, nullptr, 0, T, 1, W, s);
-    case 512: return column_w512<512, false>(spec, spec, nullptr, 0, T, 1, W, s);
+    case 128: return column_w512<128, false>(spec, spec, nullptr, 0, T, 1, W, nullptr, s);
+    case 256: return column_w512<256, false>(spec, spec, nullptr, 0, T, 1, W, nullptr, s);
+    case 384: return column_w512<384, false>(spec, spec, nullptr, 0, T, 1, W, nullptr, s);
+    case 512: return column_w512<512, false>(spec, spec, nullptr, 0, T, 1, W, nullptr, s);
   }
   return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_column_flip_w512(const float2 *spec, float2 *g, const int8_t *sign, int t0,
-                                    int nt, int D, int H, int W, cudaStream_t s) {
+                                    int nt, int D, int H, int W, const int2 *live,
+                                    cudaStream_t s) {
   switch (H) {
-    case 128: return column_w512<128, true>(spec, g, sign, t0, nt, D, W, s);
-    case 256: return column_w512<256, true>(spec, g, sign, t0, nt, D, W, s);
-    case 384: return column_w512<384, true>(spec, g, sign, t0, nt, D, W, s);
-    case 512: return column_w512<512, true>(spec, g, sign, t0, nt, D, W, s);
+    case 128: return column_w512<128, true>(spec, g, sign, t0, nt, D, W, live, s);
+    case 256: return column_w512<256, true>(spec, g, sign, t0, nt, D, W, live, s);
+    case 384: return column_w512<384, true>(spec, g, sign, t0, nt, D, W, live, s);
+    case 512: return column_w512<512, true>(spec, g, sign, t0, nt, D, W, live, s);
   }
   return cudaErrorInvalidValue;
 }

@@ -133,6 +133,13 @@ class FbpPlan(FbpDesc):
     def launches_per_execute(self):
         return self._lib.gnc_fbp_launches(self._h)
 
+    def live_slabs(self, stream=None):
+        """int32 (T, 2): per tilt the first and last slab any voxel reads; the
+        flip and filter skip the other (tilt, slab) pairs."""
+        out = np.empty((self.T, 2), np.int32)
+        _lib.check(self._lib.gnc_fbp_live_slabs(self._h, out.ctypes.data, _stream(stream)))
+        return out
+
     @property
     def backprojector(self):
         """0: the exact backprojection kernel; 2 or 4: the fast kernel and its

@@ -242,6 +242,11 @@ GNC_API int gnc_fbp_slab_map(gnc_fbp_plan *plan, int32_t *d_out, void *stream);
 GNC_API int gnc_fbp_sign_table(gnc_fbp_plan *plan, int8_t *d_out, void *stream);
 /* Number of kernel launches one gnc_fbp_execute enqueues. */
 GNC_API int gnc_fbp_launches(const gnc_fbp_plan *plan);
+/* Per tilt, the first and last defocus slab any voxel of the volume reads
+ * (h_out: 2 * T int32, host), as the plan computes them on the device; the
+ * phase flip and ramp filter of gnc_fbp_execute skip the other (tilt, slab)
+ * pairs, whose staged rows are then left unwritten.  Synchronises `stream`. */
+GNC_API int gnc_fbp_live_slabs(gnc_fbp_plan *plan, int32_t *h_out, void *stream);
 /* Which backprojection kernel gnc_fbp_execute runs for this plan: 0 the
  * exact kernel (rows with different centres, an odd detector width or too
  * many slabs per tile), else the fast kernel's slab capacity per tile (2 or 4);

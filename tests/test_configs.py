@@ -133,17 +133,21 @@ def test_3dctf_ndf10_1024(G, series_3dctf, staging):
         assert rel_l2(got, ref64) < FP16_TOL
 
 
-@pytest.fixture(scope="module")
-def series_large_3dctf(G, oracle):
-    """The large 3D-CTF geometry on 5 tilts of seeded noise, and both oracles on
-    three 8-row bands (rows 0-7, 2044-2051, 4088-4095)."""
+@pytest.fixture(scope="module", params=["phantom", "noise"])
+def series_large_3dctf(request, G, oracle):
+    """The large 3D-CTF geometry on 5 tilts, and both oracles on three 8-row
+    bands (rows 0-7, 2044-2051, 4088-4095).  Inputs: the configuration's own
+    data (a seeded 20000-blob phantom imaged through the CTF, with noise), and
+    white noise."""
     T, n, Z, ps, df, D = 5, 4096, 512, 0.8, 40000.0, 20
     ang = np.deg2rad(np.linspace(-60, 60, T)).astype(np.float32)
     c = G.get_centre((T, n, n), None, False)
     mn, mx, step, nd = G.get_defocus_steps(df, D, None, n, c, ps)
     assert nd == D
-    rng = np.random.default_rng(17)
-    proj = rng.standard_normal((T, n, n)).astype(np.float32)
+    if request.param == "phantom":
+        ang, proj = _series(G, T, n, Z, 20000, seed=4, defocus=df, pixel_size=ps)
+    else:
+        proj = np.random.default_rng(17).standard_normal((T, n, n)).astype(np.float32)
     ctf = oracle.ctf_stack(n, n, ps, 300, mn, nd, step, 2.7)
     rows = np.concatenate([np.arange(0, 8), np.arange(n // 2 - 4, n // 2 + 4),
                            np.arange(n - 8, n)])
@@ -154,7 +158,7 @@ def series_large_3dctf(G, oracle):
     desc = dict(grid_height=Z, centre=c, pixel_size=ps, correct=True, num_defocus=nd,
                 slab_defocus=G.api.slab_defoci(mn, nd, step), min_defocus=float(mn - df),
                 max_defocus=float(mx - df), energy=300.0, spherical_aberration=2.7)
-    return ang, proj, desc, rows, ref32, ref64
+    return request.param, ang, proj, desc, rows, ref32, ref64
 
 
 @pytest.mark.parametrize("staging", ["f32", "f16"])
@@ -163,10 +167,16 @@ def test_large_3dctf_ndf20_4096_bands_vs_oracles(G, series_large_3dctf, staging)
     the 4096-point block transforms, the packed signs of 4096 rows and the
     20-slab map against the reference CPU path (float oracle) and the FP64
     oracle (correct.cu:30-86 / correct.cpp:43-89, filter.cpp:61-97,
-    reconstructor.cpp:14-90)."""
+    reconstructor.cpp:14-90).
+
+    On white noise the reference's own float arithmetic is 1.4e-4 from FP64 at
+    this width (its float detector coordinate near 2048 px carries 2^-12 px,
+    and noise makes neighbouring pixels differ by their full size), so there
+    the FP32 form is held to the reference CPU path at 1e-4 and to FP64 at the
+    reference's own distance (plus 5 %)."""
     import torch
 
-    ang, proj, desc, rows, ref32, ref64 = series_large_3dctf
+    kind, ang, proj, desc, rows, ref32, ref64 = series_large_3dctf
     T, n = proj.shape[0], proj.shape[2]
     plan = G.FbpPlan(T, n, n, ang, staging=staging, **desc)
     vol = torch.empty(plan.volume_shape, dtype=torch.float32, device="cuda")
@@ -176,17 +186,14 @@ def test_large_3dctf_ndf20_4096_bands_vs_oracles(G, series_large_3dctf, staging)
     plan.close()
     del vol
     torch.cuda.empty_cache()
-    for b in range(3):  # each band on its own, then all together
-        sl = slice(8 * b, 8 * b + 8)
+    tol64 = FP32_TOL if kind == "phantom" else max(FP32_TOL, 1.05 * rel_l2(ref32, ref64))
+    for b in list(range(3)) + [None]:  # each band on its own, then all together
+        sl = slice(8 * b, 8 * b + 8) if b is not None else slice(None)
         if staging == "f32":
             assert rel_l2(got[sl], ref32[sl]) < FP32_TOL, b
-            assert rel_l2(got[sl], ref64[sl]) < FP32_TOL, b
+            assert rel_l2(got[sl], ref64[sl]) < tol64, b
         else:
             assert rel_l2(got[sl], ref64[sl]) < FP16_TOL, b
-    if staging == "f32":
-        assert rel_l2(got, ref32) < FP32_TOL
-    else:
-        assert rel_l2(got, ref64) < FP16_TOL
 
 
 def test_large_plain_fbp_rows_match_a_band_plan(G):

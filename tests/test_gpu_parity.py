@@ -178,6 +178,25 @@ def test_slab_map_bit_exact(torch, oracle, D, Z):
     np.testing.assert_array_equal(out.cpu().numpy(), ref)
 
 
+# The phase flip and the ramp filter run only for the (tilt, slab) pairs some
+# voxel reads: per tilt the slab range at the volume's corners, which must be
+# exactly the range of the reference's slab index over the whole volume
+# (reconstructor.cpp:66-72).  At the 3D-CTF benchmark's shape (1024 px,
+# Z = 300, ten slabs) the low tilts read fewer than half of the slabs.
+@pytest.mark.parametrize("T,W,Z,D", [(17, 48, 40, 5), (13, 64, 33, 10), (61, 1024, 300, 10),
+                                     (9, 256, 256, 4)])
+def test_live_slabs_match_slab_map(torch, oracle, T, W, Z, D):
+    plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=T, H=4, W=W, Z=Z, D=D)
+    live = plan.live_slabs()
+    ref = oracle.slab_index_map(W, D, (Z, W), ang, float(c[0]), 1.0, mn, mx).reshape(T, -1)
+    np.testing.assert_array_equal(live[:, 0], ref.min(axis=1))
+    np.testing.assert_array_equal(live[:, 1], ref.max(axis=1))
+    if (W, Z, D) == (1024, 300, 10):
+        pairs = int((live[:, 1] - live[:, 0] + 1).sum())
+        assert pairs < 0.85 * T * D  # the skipped share this shape relies on
+        assert (live[T // 2, 1] - live[T // 2, 0] + 1) <= 4  # the untilted view
+
+
 def _staged_from_rows(filtered_rows, H):
     """Per-row filtered sinograms (H, D, T, N) -> staged pairs (H2, D, T, N, 2)."""
     Hh, D, T, N = filtered_rows.shape
