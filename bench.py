@@ -44,9 +44,24 @@ WL = dict(T=61, H=1024, W=1024, Z=300, D=10, pixel_size=1.0, defocus=30000.0, en
           cs_mm=2.7, blobs=2000, seed=3, tilt_max=60.0, noise=0.1, ctf=True)
 WORKLOAD_NAME = ("3D CTF ndf=10: 61 tilts +-60 deg, 1024x1024 projections at 1.0 A/px, "
                  "300 kV, Cs 2.7 mm, df 30000 A, volume 1024x1024x300")
-# DRAM traffic of one k_bp_fast launch on this workload, from the ncu capture
-# summarised in profiles/k_bp_fast_3dctf_ndf10.md (bytes read + written).
-BP_TRAFFIC_BYTES = {"f32": 2.330e9, "f16": 2.332e9}
+# DRAM bytes (read + written) of one backprojection launch on this workload,
+# from an ncu capture whose summary (command included) is committed beside the
+# other profiles; the line names the file it came from.
+TRAFFIC_CAPTURE = os.path.join("profiles", "k_bp_fast_dram_3dctf_ndf10.txt")
+
+
+def bp_traffic(form):
+    """(bytes per launch, source) from the capture summary, or (None, reason)."""
+    path = os.path.join(REPO, TRAFFIC_CAPTURE)
+    try:
+        with open(path) as f:
+            for line in f:
+                parts = dict(kv.split("=", 1) for kv in line.split() if "=" in kv)
+                if parts.get("form") == form and "dram_bytes_per_launch" in parts:
+                    return float(parts["dram_bytes_per_launch"]), TRAFFIC_CAPTURE
+    except OSError:
+        pass
+    return None, f"no capture of the {form} backprojector in {TRAFFIC_CAPTURE}"
 
 
 def angles_rad():
@@ -280,6 +295,7 @@ def run_ours(args, rank, world, dist):
     vol_bytes = WL["H"] * WL["Z"] * WL["W"] * 4
     bp_alg = staged_bytes + vol_bytes
     bp_ms = res["f32"][1]
+    traffic, traffic_src = bp_traffic("f32")
     achieved = bp_alg / (bp_ms * 1e-3) / 1e9
     # the backprojector's binding resource: shared-memory loads, two 8-byte
     # pixel pairs per (voxel, row pair, tilt) = 8 bytes per voxel-tilt, against
@@ -340,7 +356,8 @@ def run_ours(args, rank, world, dist):
             "peak_source": peak_src,
             "unit": "GB/s",
             "frac": round(achieved / hbm_peak, 4),
-            "traffic": BP_TRAFFIC_BYTES["f32"] if args.case == "3dctf" else None,
+            "traffic": traffic if args.case == "3dctf" else None,
+            "traffic_source": traffic_src if args.case == "3dctf" else "no capture for this case",
             "algorithmic_bytes": bp_alg,
             "kernel_ms": round(bp_ms, 4),
             "binding": {
@@ -504,10 +521,10 @@ def run_serving(dev):
     }
 
 
-def oracle_sample(proj, vols, nrows=8):
-    """FP32 and FP64 oracle on a sample of rows of the same series: parity of
-    both GPU forms, and the timed CPU baseline (correction of every tilt plus
-    filter and backprojection of the sampled rows, extrapolated)."""
+def cpu_inputs(proj=None):
+    """The CPU arms' inputs: the oracle's CTF stack and slab range for the
+    workload, and the projections (the bench's own, or a seeded stand-in of
+    the same shape: the oracle's run time does not depend on the values)."""
     from oracle import oracle as O
 
     c, mn, mx, step, nd = slab_setup()
@@ -516,22 +533,56 @@ def oracle_sample(proj, vols, nrows=8):
                        WL["cs_mm"]) if WL["ctf"] else None)
     if ctf is None:
         mn = mx = df
-    p = proj.cpu().numpy()
+    if proj is None:
+        rng = np.random.default_rng(WL["seed"])
+        proj = rng.standard_normal((WL["T"], WL["H"], WL["W"])).astype(np.float32)
+    return proj, c, ctf, float(mn - df), float(mx - df)
+
+
+def cpu_sample(p, c, ctf, rel_mn, rel_mx, threads):
+    """One bounded sample of the reference's CPU algorithm (the float oracle,
+    OpenMP on `threads` host threads): CTF correction of min(T, threads) tilts
+    (one per thread) and ramp filter + backprojection of `threads` Y rows (one
+    per thread) of every tilt.  Returns the measured sample time and the whole
+    series' time extrapolated from it (correction scales with the tilts, the
+    rest with the rows)."""
+    from oracle import oracle as O
+
     ang = angles_rad()
+    kt = min(WL["T"], threads)
+    nrows = min(WL["H"], threads)
+    y0 = WL["H"] // 2 - nrows // 2
+    t0 = time.perf_counter()
+    if ctf is not None:
+        O.fbp_ctf(p, ang, c, WL["pixel_size"], ctf, rel_mn, rel_mx, Z=WL["Z"], rows=(0, 0),
+                  tilts=(0, kt), nthreads=threads)
+    t1 = time.perf_counter()
+    O.fbp_ctf(p, ang, c, WL["pixel_size"], ctf, rel_mn, rel_mx, Z=WL["Z"],
+              rows=(y0, y0 + nrows), tilts=(0, 0), nthreads=threads)
+    t2 = time.perf_counter()
+    series = (t1 - t0) * WL["T"] / kt + (t2 - t1) * WL["H"] / nrows
+    desc = ((f"CTF correction of {kt} of {WL['T']} tilts ({t1 - t0:.2f} s) and " if ctf is not None
+             else "") + f"ramp filter + backprojection of {nrows} of {WL['H']} rows "
+            f"({t2 - t1:.2f} s) on {threads} threads, extrapolated to the whole series")
+    return t2 - t0, series, desc
+
+
+def oracle_sample(proj, vols):
+    """Parity of both GPU forms against the FP32 and FP64 oracles on a band of
+    rows of the same series (every tilt corrected), and the CPU baseline: one
+    cpu_sample of the reference's algorithm, as the reference arm times it."""
+    from oracle import oracle as O
+
+    threads = os.cpu_count() or 1
+    p, c, ctf, rel_mn, rel_mx = cpu_inputs(proj.cpu().numpy())
+    ang = angles_rad()
+    nrows = 8
     y0 = WL["H"] // 2 - nrows // 2
     rows = (y0, y0 + nrows)
-    threads = os.cpu_count() or 1
-    t0 = time.perf_counter()
-    O.fbp_ctf(p, ang, c, WL["pixel_size"], ctf, float(mn - df), float(mx - df), Z=WL["Z"],
-              rows=(0, 0), nthreads=threads)
-    t_corr = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    v32 = O.fbp_ctf(p, ang, c, WL["pixel_size"], ctf, float(mn - df), float(mx - df), Z=WL["Z"],
-                    rows=rows, nthreads=threads)
-    t_both = time.perf_counter() - t0
-    t_rows = max(t_both - t_corr, 1e-9)
-    v64 = O.fbp_ctf(p, ang, c, WL["pixel_size"], ctf, float(mn - df), float(mx - df), Z=WL["Z"],
-                    rows=rows, precision="f64", nthreads=threads)
+    v32 = O.fbp_ctf(p, ang, c, WL["pixel_size"], ctf, rel_mn, rel_mx, Z=WL["Z"], rows=rows,
+                    nthreads=threads)
+    v64 = O.fbp_ctf(p, ang, c, WL["pixel_size"], ctf, rel_mn, rel_mx, Z=WL["Z"], rows=rows,
+                    precision="f64", nthreads=threads)
     sl = slice(*rows)
     r64 = v64[sl]
     r32 = v32[sl]
@@ -549,18 +600,15 @@ def oracle_sample(proj, vols, nrows=8):
         "f32_max_abs_vs_fp64": float(np.abs(g32 - r64).max()),
         "reference_cpu_vs_fp64_rel_l2": rel(r32, r64),
     }
-    full_s = t_corr + t_rows * WL["H"] / nrows
+    sample_s, series_s, desc = cpu_sample(p, c, ctf, rel_mn, rel_mx, threads)
     cpu = {
-        "value": round(voxel_tilts() / full_s / 1e9, 4),
+        "value": round(voxel_tilts() / series_s / 1e9, 4),
         "unit": UNIT,
         "cores": threads,
         "kind": "port",
-        "sample": (f"oracle restatement of the reference CPU path (float, OpenMP, {threads} "
-                   f"threads): "
-                   + (f"CTF correction of all {WL['T']} tilts ({t_corr:.2f} s) plus "
-                      if WL["ctf"] else "")
-                   + f"filter and backprojection of {nrows} of {WL['H']} rows ({t_rows:.2f} s), "
-                   f"extrapolated to all rows: {full_s:.2f} s per series"),
+        "sample_ms": round(sample_s * 1e3, 1),
+        "series_ms_extrapolated": round(series_s * 1e3, 1),
+        "sample": "oracle restatement of the reference CPU path (float): " + desc,
     }
     return parity, cpu
 
@@ -569,53 +617,34 @@ def oracle_sample(proj, vols, nrows=8):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    from oracle import oracle as O
     import guanaco_gb300 as G  # noqa: F401  (host helpers only: defocus steps)
 
     threads = os.cpu_count() or 1
-    c, mn, mx, step, nd = slab_setup()
-    df = WL["defocus"]
-    rng = np.random.default_rng(WL["seed"])
-    # the sample needs only its tilts and rows: a seeded stand-in with the
-    # workload's shape (the timing does not depend on the values)
-    p = rng.standard_normal((WL["T"], WL["H"], WL["W"])).astype(np.float32)
-    ctf = (O.ctf_stack(WL["W"], WL["H"], WL["pixel_size"], WL["energy"], mn, nd, step,
-                       WL["cs_mm"]) if WL["ctf"] else None)
-    if ctf is None:
-        mn = mx = df
-    ang = angles_rad()
-    k_tilts = min(WL["T"], threads)
-    m_rows = threads
-
-    def step_once():
-        t0 = time.perf_counter()
-        O.fbp_ctf(p, ang, c, WL["pixel_size"], ctf, float(mn - df), float(mx - df), Z=WL["Z"],
-                  rows=(0, 0), tilts=(0, k_tilts), nthreads=threads)
-        t1 = time.perf_counter()
-        O.fbp_ctf(p, ang, c, WL["pixel_size"], ctf, float(mn - df), float(mx - df), Z=WL["Z"],
-                  rows=(0, m_rows), tilts=(0, 0), nthreads=threads)
-        t2 = time.perf_counter()
-        return (t1 - t0) * WL["T"] / k_tilts + (t2 - t1) * WL["H"] / m_rows
-
+    p, c, ctf, rel_mn, rel_mx = cpu_inputs()
     for _ in range(args.warmup):
-        step_once()
-    per = [step_once() for _ in range(args.steps)]
-    full_s = sum(per) / len(per)
-    value = voxel_tilts() / full_s / 1e9
+        cpu_sample(p, c, ctf, rel_mn, rel_mx, threads)
+    runs = [cpu_sample(p, c, ctf, rel_mn, rel_mx, threads) for _ in range(args.steps)]
+    sample_s = sum(r[0] for r in runs) / len(runs)
+    series_s = sum(r[1] for r in runs) / len(runs)
+    value = voxel_tilts() / series_s / 1e9
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "impl": "reference",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(full_s * 1e3, 2), "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": round(sample_s * 1e3, 2),
+        "series_ms_extrapolated": round(series_s * 1e3, 2),
+        "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, workload shape)",
         "config": {"workload": WORKLOAD_NAME, "tilts": WL["T"],
                    "projection": [WL["H"], WL["W"]], "volume": [WL["H"], WL["W"], WL["Z"]],
                    "ndf": WL["D"], "staging": "f32", "parallelism": "host threads"},
         "cpu_baseline": {
             "value": round(value, 4), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": (f"per step: CTF correction of {k_tilts} of {WL['T']} tilts and filter + "
-                       f"backprojection of {m_rows} of {WL['H']} rows, extrapolated to the "
-                       "whole series; oracle restatement of the reference CPU path (the "
-                       "reference itself needs FFTW and its source tree, absent on this host)"),
+            "sample_ms": round(sample_s * 1e3, 1),
+            "series_ms_extrapolated": round(series_s * 1e3, 1),
+            "sample": ("per step, one bounded sample: " + runs[-1][2] + "; value = the series' "
+                       "voxel-tilts over the extrapolated series time; oracle restatement of "
+                       "the reference CPU path (the reference itself needs FFTW and its source "
+                       "tree, absent on this host)"),
         },
         "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
