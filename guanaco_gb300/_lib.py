@@ -22,6 +22,7 @@ GNC_ERR_PENDING = 6
 
 GNC_STAGE_F32 = 0
 GNC_STAGE_F16 = 1
+GNC_STAGE_F16T = 2
 GNC_INPUT_RAW = 0
 GNC_INPUT_CORRECTED = 1
 

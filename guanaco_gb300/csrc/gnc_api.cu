@@ -178,8 +178,10 @@ struct gnc_fbp_plan {
   // chunk's row stage; events: fork, flip done (per buffer), rows done (per buffer)
   cudaStream_t s_flip = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_flip[2] = {}, ev_rows[2] = {};
-  void *staged = nullptr;   // (Y2, D, T, W) pairs
+  void *staged = nullptr;   // (Y2, D, T, W) pairs, or F16T rows (D, T, H, W)
   int8_t *row_exp = nullptr;
+  int8_t *tilt_exp = nullptr;  // F16T: (T) per-tilt exponents
+  TcMap tc_map{};              // F16T: TMA descriptor of the staged rows
   int8_t *sign = nullptr;   // (D, H, W/2 + 1)
   int2 *live = nullptr;     // (T): first and last slab the volume reads (CTF, D > 1)
   // everything that differs between two requests of the same shape, in one
@@ -214,6 +216,7 @@ static void plan_free(gnc_fbp_plan *p) {
   if (p->s_flip) cudaStreamDestroy(p->s_flip);
   cudaFree(p->staged);
   cudaFree(p->row_exp);
+  cudaFree(p->tilt_exp);
   cudaFree(p->sign);
   cudaFree(p->live);
   cudaFree(p->params);
@@ -238,6 +241,9 @@ static BpArgs bp_args(const gnc_fbp_plan *p, float *vol) {
   BpArgs a{};
   a.staged = p->staged;
   a.row_exp = p->row_exp;
+  a.tilt_exp = p->tilt_exp;
+  a.stack_h = p->H;
+  a.y_begin = 0;
   a.staging = p->staging;
   a.Y = p->H;
   a.D = p->D;
@@ -322,7 +328,8 @@ int desc_check(const gnc_fbp_desc *d) {
   GNC_REQUIRE(d->min_defocus <= d->max_defocus);
   GNC_REQUIRE(d->num_defocus == 1 || d->max_defocus > d->min_defocus);
   GNC_REQUIRE(d->input == GNC_INPUT_RAW || d->input == GNC_INPUT_CORRECTED);
-  GNC_REQUIRE(d->staging == GNC_STAGE_F32 || d->staging == GNC_STAGE_F16);
+  GNC_REQUIRE(d->staging == GNC_STAGE_F32 || d->staging == GNC_STAGE_F16 ||
+              d->staging == GNC_STAGE_F16T);
   const bool ctf = d->input == GNC_INPUT_RAW && d->correct;
   GNC_REQUIRE(ctf || d->input == GNC_INPUT_CORRECTED || d->num_defocus == 1);
   if (ctf) GNC_REQUIRE(d->slab_defocus != nullptr);
@@ -335,6 +342,24 @@ int desc_check(const gnc_fbp_desc *d) {
     return GNC_ERR_UNSUPPORTED;
   }
   return GNC_OK;
+}
+
+// The staging a plan for d uses: F16T (FP16 rows, tensor-core backprojection)
+// only where that kernel takes the geometry, else the FP16 records.
+int effective_staging(const gnc_fbp_desc *d) {
+  if (d->staging != GNC_STAGE_F16T) return d->staging;
+  float dscale, doffset;
+  const float mn = d->num_defocus > 1 ? d->min_defocus : 0.f;
+  const float mx = d->num_defocus > 1 ? d->max_defocus : 0.f;
+  defocus_scale(d->num_defocus, d->pixel_size, mn, mx, &dscale, &doffset);
+  bool uniform = true;
+  if (d->centre)
+    for (size_t y = 1; y < d->height; ++y)
+      if (d->centre[y] != d->centre[0]) uniform = false;
+  return backproject_tc_supported((int)d->width, (int)d->num_angles, dscale,
+                                  (int)d->num_defocus, uniform)
+             ? GNC_STAGE_F16T
+             : GNC_STAGE_F16;
 }
 
 // Device bytes gnc_fbp_plan_create allocates for d (the same sizes, without
@@ -350,8 +375,12 @@ size_t plan_bytes(const gnc_fbp_desc *d) {
     b += T * H * half * sizeof(float2) + 2 * chunk * D * H * half * sizeof(float2) +
          sign_table_bytes((int)D, (int)H, (int)W) + (D > 1 ? T * sizeof(int2) : 0);
   }
-  b += (Y2 * D * T * W + 8) * kStagedPixelBytes;
-  if (d->staging == GNC_STAGE_F16) b += Y2 * D * T * 2;
+  const int staging = effective_staging(d);
+  if (staging == GNC_STAGE_F16T)
+    b += (D * T * H * W + 64) * 2 + T;
+  else
+    b += (Y2 * D * T * W + 8) * kStagedPixelBytes;
+  if (staging == GNC_STAGE_F16) b += Y2 * D * T * 2;
   const size_t in_elems = T * (d->input == GNC_INPUT_CORRECTED ? D : 1) * H * W;
   b += (in_elems + H * d->grid_height * d->grid_width) * sizeof(float);
   return b;
@@ -369,7 +398,7 @@ std::string plan_key(const gnc_fbp_desc *d) {
     for (size_t y = 1; y < d->height; ++y)
       if (d->centre[y] != d->centre[0]) uniform = false;
   BpArgs a{};
-  a.staging = d->staging;
+  a.staging = effective_staging(d);
   a.N = (int)d->width;
   a.D = (int)d->num_defocus;
   a.dscale = dscale;
@@ -377,7 +406,7 @@ std::string plan_key(const gnc_fbp_desc *d) {
   char buf[256];
   snprintf(buf, sizeof buf, "%zu,%zu,%zu,%zu,%zu,%zu,%d,%d,%d,%d", d->num_angles, d->height,
            d->width, d->grid_height, d->grid_width, d->num_defocus, d->input,
-           (d->input == GNC_INPUT_RAW && d->correct) ? 1 : 0, d->staging,
+           (d->input == GNC_INPUT_RAW && d->correct) ? 1 : 0, a.staging,
            backproject_fast_variant(a));
   return buf;
 }
@@ -465,7 +494,7 @@ int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
   p->Y2 = (p->H + 1) / 2;
   p->input = d->input;
   p->correct = ctf ? 1 : 0;
-  p->staging = d->staging;
+  p->staging = gnc::effective_staging(d);
   p->pixel_size = d->pixel_size;
   p->min_def = d->num_defocus > 1 ? d->min_defocus : 0.f;
   p->max_def = d->num_defocus > 1 ? d->max_defocus : 0.f;
@@ -499,13 +528,21 @@ int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
     if (e == cudaSuccess) e = dalloc(p, &p->sign, sign_table_bytes(p->D, p->H, p->W));
     if (e == cudaSuccess && p->D > 1) e = dalloc(p, &p->live, (size_t)p->T);
   }
-  // +8 pixels: a 16-byte aligned bulk copy of the last row may run past its end
-  const size_t elems = (size_t)p->Y2 * p->D * p->T * p->W + 8;
-  if (e == cudaSuccess)
-    e = p->staging == GNC_STAGE_F16 ? dalloc(p, (uint2 **)&p->staged, elems)
-                                    : dalloc(p, (float2 **)&p->staged, elems);
-  if (e == cudaSuccess && p->staging == GNC_STAGE_F16)
-    e = dalloc(p, &p->row_exp, (size_t)p->Y2 * p->D * p->T * 2);
+  if (p->staging == GNC_STAGE_F16T) {
+    // plain FP16 rows (D, T, H, W) read by TMA tiles, and one exponent per tilt
+    const size_t elems = (size_t)p->D * p->T * p->H * p->W + 64;
+    if (e == cudaSuccess) e = dalloc(p, (__half **)&p->staged, elems);
+    if (e == cudaSuccess) e = dalloc(p, &p->tilt_exp, (size_t)p->T);
+    if (e == cudaSuccess) e = make_tc_map(p->staged, p->D, p->T, p->H, p->W, &p->tc_map);
+  } else {
+    // +8 pixels: a 16-byte aligned bulk copy of the last row may run past its end
+    const size_t elems = (size_t)p->Y2 * p->D * p->T * p->W + 8;
+    if (e == cudaSuccess)
+      e = p->staging == GNC_STAGE_F16 ? dalloc(p, (uint2 **)&p->staged, elems)
+                                      : dalloc(p, (float2 **)&p->staged, elems);
+    if (e == cudaSuccess && p->staging == GNC_STAGE_F16)
+      e = dalloc(p, &p->row_exp, (size_t)p->Y2 * p->D * p->T * 2);
+  }
   if (e == cudaSuccess) e = dalloc(p, &p->err, 1);
   if (e == cudaSuccess) e = cudaMemset(p->err, 0, sizeof(int));
   if (e != cudaSuccess) {
@@ -563,10 +600,19 @@ static int flip_rows(gnc_fbp_plan *p, RowStageArgs r, int t_begin, int t_end, fl
   return GNC_OK;  // s has waited for every flip: the side stream is joined
 }
 
-// Raw or corrected input -> staged filtered rows (the plan's staging buffer).
-int gnc_fbp_stage(gnc_fbp_plan *p, const float *d_input, void *stream) {
-  GNC_REQUIRE(p != nullptr && d_input != nullptr);
-  cudaStream_t s = (cudaStream_t)stream;
+// F16T: the per-tilt exponents of input tilts [t0, t0 + nt) (input holds
+// every tilt, (T, per_tilt) floats).
+static cudaError_t tilt_exponents(gnc_fbp_plan *p, const float *input, int t0, int nt,
+                                  cudaStream_t s) {
+  if (p->staging != GNC_STAGE_F16T) return cudaSuccess;
+  const size_t per_tilt = (size_t)(p->input == GNC_INPUT_CORRECTED ? p->D : 1) * p->H * p->W;
+  // the unnormalised correction multiplies the L2 norm by at most H W
+  const double gain = p->correct ? (double)p->H * p->W : 1.0;
+  return launch_tilt_exponents(input, per_tilt, t0, nt, p->tilt_factor, gain, p->tilt_exp, s);
+}
+
+// The staged-output arguments of the row stage.
+static RowStageArgs stage_args(const gnc_fbp_plan *p) {
   RowStageArgs r{};
   r.D = p->D;
   r.H = p->H;
@@ -578,6 +624,25 @@ int gnc_fbp_stage(gnc_fbp_plan *p, const float *d_input, void *stream) {
   r.staging = p->staging;
   r.staged = p->staged;
   r.row_exp = p->row_exp;
+  r.tilt_exp = p->tilt_exp;
+  return r;
+}
+
+// The fast backprojector of the plan's staging (tensor cores for F16T), or
+// the exact kernel for rows with different centres or when asked for.
+static cudaError_t backproject(const gnc_fbp_plan *p, const BpArgs &a, bool exact,
+                               cudaStream_t s, const TcMap *map = nullptr) {
+  if (exact || !p->uniform_centre) return launch_backproject_exact(a, s);
+  if (a.staging == GNC_STAGE_F16T) return launch_backproject_tc(a, map ? *map : p->tc_map, s);
+  return launch_backproject_fast(a, s);
+}
+
+// Raw or corrected input -> staged filtered rows (the plan's staging buffer).
+int gnc_fbp_stage(gnc_fbp_plan *p, const float *d_input, void *stream) {
+  GNC_REQUIRE(p != nullptr && d_input != nullptr);
+  cudaStream_t s = (cudaStream_t)stream;
+  RowStageArgs r = stage_args(p);
+  GNC_CUDA(tilt_exponents(p, d_input, 0, p->T, s));
   if (p->correct) {
     GNC_CUDA(launch_sign_table(p->sargs, p->sign, s));
     GNC_CUDA(launch_sign_pack(p->sign, p->D, p->H, p->W, s));
@@ -603,26 +668,27 @@ int gnc_fbp_stage(gnc_fbp_plan *p, const float *d_input, void *stream) {
 int gnc_fbp_backproject(gnc_fbp_plan *p, float *d_volume, int exact, void *stream) {
   GNC_REQUIRE(p != nullptr && d_volume != nullptr);
   cudaStream_t s = (cudaStream_t)stream;
-  BpArgs a = bp_args(p, d_volume);
-  if (exact || !p->uniform_centre)
-    GNC_CUDA(launch_backproject_exact(a, s));
-  else
-    GNC_CUDA(launch_backproject_fast(a, s));
+  GNC_CUDA(backproject(p, bp_args(p, d_volume), exact != 0, s));
   return GNC_OK;
 }
 
 int gnc_fbp_backproject_staged(gnc_fbp_plan *p, const void *d_staged, const int8_t *d_row_exp,
                                float *d_volume, int exact, void *stream) {
   GNC_REQUIRE(p != nullptr && d_staged != nullptr && d_volume != nullptr);
-  GNC_REQUIRE(p->staging != GNC_STAGE_F16 || d_row_exp != nullptr);
+  GNC_REQUIRE(p->staging == GNC_STAGE_F32 || d_row_exp != nullptr);
   cudaStream_t s = (cudaStream_t)stream;
   BpArgs a = bp_args(p, d_volume);
   a.staged = d_staged;
   a.row_exp = d_row_exp;
-  if (exact || !p->uniform_centre)
-    GNC_CUDA(launch_backproject_exact(a, s));
-  else
-    GNC_CUDA(launch_backproject_fast(a, s));
+  if (p->staging == GNC_STAGE_F16T) {  // F16T: the exponents are per tilt
+    a.row_exp = nullptr;
+    a.tilt_exp = d_row_exp;
+    TcMap map;
+    GNC_CUDA(make_tc_map(d_staged, p->D, p->T, p->H, p->W, &map));
+    GNC_CUDA(backproject(p, a, exact != 0, s, &map));
+    return GNC_OK;
+  }
+  GNC_CUDA(backproject(p, a, exact != 0, s));
   return GNC_OK;
 }
 
@@ -685,17 +751,7 @@ static int execute_host_pipelined(gnc_fbp_plan *p, const float *h_input, float *
                              n * per_tilt * sizeof(float), cudaMemcpyHostToDevice, p->s_in));
     GNC_CUDA(cudaEventRecord(ev_in[g], p->s_in));
   }
-  RowStageArgs r{};
-  r.D = p->D;
-  r.H = p->H;
-  r.N = p->W;
-  r.T = p->T;
-  r.ramp = 1;
-  r.tilt_factor = p->tilt_factor;
-  r.out_staged = 1;
-  r.staging = p->staging;
-  r.staged = p->staged;
-  r.row_exp = p->row_exp;
+  RowStageArgs r = stage_args(p);
   if (p->correct) {
     GNC_CUDA(launch_sign_table(p->sargs, p->sign, s));
     GNC_CUDA(launch_sign_pack(p->sign, p->D, p->H, p->W, s));
@@ -711,6 +767,7 @@ static int execute_host_pipelined(gnc_fbp_plan *p, const float *h_input, float *
   for (int g = 0, t0 = 0; t0 < p->T; ++g, t0 += group) {
     const int n = std::min(group, p->T - t0);
     GNC_CUDA(cudaStreamWaitEvent(s, ev_in[g], 0));
+    GNC_CUDA(tilt_exponents(p, p->io_in, t0, n, s));
     if (p->correct) {
       float2 *spec = p->spec + (size_t)t0 * p->H * half;
       GNC_CUDA(launch_rfft_rows(p->io_in + (size_t)t0 * per_tilt, spec, n, p->H, p->W, s));
@@ -760,13 +817,14 @@ static int execute_host_pipelined(gnc_fbp_plan *p, const float *h_input, float *
     BpArgs a = bp_args(p, p->io_out + (size_t)y0 * plane);
     const size_t pair0 = (size_t)(y0 / 2) * p->D * p->T;
     a.Y = ny;
-    a.staged = (const unsigned char *)p->staged + pair0 * p->W * pb;
-    a.row_exp = p->row_exp ? p->row_exp + 2 * pair0 : nullptr;
+    if (p->staging == GNC_STAGE_F16T) {
+      a.y_begin = y0;  // F16T rows stay whole: the launch starts at stack row y0
+    } else {
+      a.staged = (const unsigned char *)p->staged + pair0 * p->W * pb;
+      a.row_exp = p->row_exp ? p->row_exp + 2 * pair0 : nullptr;
+    }
     a.offset = p->offset + (size_t)y0 * p->T;
-    if (!p->uniform_centre)
-      GNC_CUDA(launch_backproject_exact(a, s));
-    else
-      GNC_CUDA(launch_backproject_fast(a, s));
+    GNC_CUDA(backproject(p, a, false, s));
     GNC_CUDA(cudaEventRecord(ev_bp[j], s));
     GNC_CUDA(cudaStreamWaitEvent(p->s_out, ev_bp[j], 0));
     GNC_CUDA(cudaMemcpyAsync(h_volume + (size_t)y0 * plane, p->io_out + (size_t)y0 * plane,
@@ -834,11 +892,12 @@ int gnc_fbp_slab_map(gnc_fbp_plan *p, int32_t *d_out, void *stream) {
 
 int gnc_fbp_launches(const gnc_fbp_plan *p) {
   if (!p) return 0;
-  if (!p->correct) return 2;  // row stage, backprojection
+  const int f16t = p->staging == GNC_STAGE_F16T ? 1 : 0;  // the per-tilt exponents
+  if (!p->correct) return 2 + f16t;  // row stage, backprojection
   const int chunks = (p->T + p->chunk - 1) / p->chunk;
   // sign table (+ its packed copy, + the live slab ranges), row and column
   // transforms, per chunk flip + rows, BP
-  return 3 + (sign_pack_used(p->H) ? 1 : 0) + (p->live ? 1 : 0) + 2 * chunks + 1;
+  return 3 + (sign_pack_used(p->H) ? 1 : 0) + (p->live ? 1 : 0) + f16t + 2 * chunks + 1;
 }
 
 int gnc_fbp_live_slabs(gnc_fbp_plan *p, int32_t *h_out, void *stream) {
@@ -857,6 +916,7 @@ int gnc_fbp_live_slabs(gnc_fbp_plan *p, int32_t *h_out, void *stream) {
 int gnc_fbp_backprojector(const gnc_fbp_plan *p) {
   if (!p) return -1;
   if (!p->uniform_centre) return 0;
+  if (p->staging == GNC_STAGE_F16T) return 16;  // the tensor-core kernel
   return backproject_fast_variant(bp_args(p, nullptr));
 }
 
@@ -882,7 +942,7 @@ int gnc_fbp_check(gnc_fbp_plan *p, void *stream) {
 int gnc_fbp_staged(gnc_fbp_plan *p, const void **d_staged, const int8_t **d_row_exp) {
   GNC_REQUIRE(p != nullptr && d_staged != nullptr);
   *d_staged = p->staged;
-  if (d_row_exp) *d_row_exp = p->row_exp;
+  if (d_row_exp) *d_row_exp = p->staging == GNC_STAGE_F16T ? p->tilt_exp : p->row_exp;
   return GNC_OK;
 }
 

@@ -185,6 +185,15 @@ __global__ void __launch_bounds__(256, 2) k_row_b4096(RowStageArgs a,
     float2 *dst = (float2 *)a.staged + (((size_t)y2 * a.D + d) * a.T + t) * kN;
 #pragma unroll
     for (int m = 0; m < 16; ++m) dst[l + 256 * m] = yv[m];
+  } else if (STAGED && F16 && a.staging == kStageF16T) {
+    // plain FP16 rows scaled by the tilt's 2^e(t)
+    const float sc = f16t_scale(a, t);
+    __half *da = f16t_row(a, d, t, ya);
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      da[l + 256 * m] = __float2half_rn(yv[m].x * sc);
+      if (hb) da[kN + l + 256 * m] = __float2half_rn(yv[m].y * sc);
+    }
   } else if (STAGED && F16) {
     // records need pixel n + 1 (another thread's): exchange through A, which
     // no thread reads any more; and the row maxima for the exponents
@@ -281,7 +290,7 @@ static cudaError_t row_b4096(const RowStageArgs &a, cudaStream_t s) {
 
 cudaError_t launch_row_stage_b4096(const RowStageArgs &a, cudaStream_t s) {
   const bool sp = a.input_spectra != 0, rm = a.ramp != 0, st = a.out_staged != 0;
-  const bool h = a.staging == kStageF16;
+  const bool h = a.staging != kStageF32;
   if (sp && rm && st && !h) return row_b4096<true, true, true, false>(a, s);
   if (sp && rm && st && h) return row_b4096<true, true, true, true>(a, s);
   if (!sp && rm && st && !h) return row_b4096<false, true, true, false>(a, s);

@@ -18,8 +18,11 @@ __device__ __forceinline__ float voxel_coord(int i, int n) {
   return (float)((double)i - 0.5 * (double)n + 0.5);
 }
 
-template <bool F16>
+// MODE: kStageF32, kStageF16 (records) or kStageF16T (plain FP16 rows, one
+// exponent per tilt)
+template <int MODE>
 __global__ void k_bp_exact(BpArgs a) {
+  constexpr bool F16 = MODE == kStageF16;
   if (a.dyn) {
     a.dscale = a.dyn[0];
     a.doffset = a.dyn[1];
@@ -42,6 +45,7 @@ __global__ void k_bp_exact(BpArgs a) {
       sa = __int_as_float((127 - a.row_exp[2 * rowi]) << 23);
       sb = __int_as_float((127 - a.row_exp[2 * rowi + 1]) << 23);
     }
+    if (MODE == kStageF16T) sa = sb = __int_as_float((127 - a.tilt_exp[t]) << 23);
     const float xc = __fmul_rn(xf, g.cos_a), zs = __fmul_rn(zf, g.sin_a);
 #pragma unroll
     for (int r = 0; r < 2; ++r) {
@@ -53,7 +57,12 @@ __global__ void k_bp_exact(BpArgs a) {
       const float tt = __fsub_rn(pixel, (float)ind);
       if (ind >= 0 && ind < a.N - 1) {
         float v0, v1;
-        if (F16) {  // the values of records ind and ind + 1
+        if (MODE == kStageF16T) {
+          const __half *row = (const __half *)a.staged +
+                              (((size_t)k * a.T + t) * a.stack_h + a.y_begin + yy) * a.N;
+          v0 = __half2float(row[ind]) * sa;
+          v1 = __half2float(row[ind + 1]) * sa;
+        } else if (F16) {  // the values of records ind and ind + 1
           const uint2 *row = (const uint2 *)a.staged + rowi * a.N;
           const unsigned u0 = row[ind].x, u1 = row[ind + 1].x;
           float2 p0 = __half22float2(*(const __half2 *)&u0);
@@ -82,9 +91,11 @@ cudaError_t launch_backproject_exact(const BpArgs &a, cudaStream_t s) {
   dim3 block(32, 8);
   dim3 grid((a.X + 31) / 32, (a.Z + 7) / 8, (a.Y + 1) / 2);
   if (a.staging == kStageF16)
-    k_bp_exact<true><<<grid, block, 0, s>>>(a);
+    k_bp_exact<kStageF16><<<grid, block, 0, s>>>(a);
+  else if (a.staging == kStageF16T)
+    k_bp_exact<kStageF16T><<<grid, block, 0, s>>>(a);
   else
-    k_bp_exact<false><<<grid, block, 0, s>>>(a);
+    k_bp_exact<kStageF32><<<grid, block, 0, s>>>(a);
   return cudaGetLastError();
 }
 

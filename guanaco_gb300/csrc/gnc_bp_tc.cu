@@ -1,0 +1,443 @@
+// Tensor-core backprojection of F16T rows (FP16, one power-of-two scale per
+// tilt) with FP32 accumulation in tensor memory.
+//
+// For one tilt, the backprojection of a set of voxels into a set of Y rows is
+// a product V[v, y] += sum_u W[v, u] S[u, y] of the interpolation weights
+// (two non-zeros per voxel: (1 - t) at the voxel's pixel floor(p), t at the
+// next one, src/libguanaco/reconstructor.cpp:76-86) and the staged rows.  A
+// block owns 128 voxels -- a 16 (x) by 8 (z) tile, compact so that for any
+// tilt they project onto at most 18 detector pixels -- and 128 Y rows.  Per
+// tilt and per defocus slab the tile reaches:
+//   * one TMA load brings the 32-pixel window [u0, u0 + 32) of the 128 rows
+//     (u0 a multiple of 8) into shared memory, 64-byte swizzled;
+//   * the 128 builder threads (one per voxel) compute the voxel's detector
+//     coordinate, floor, weight and slab with the reference's float
+//     operations, and store its 32 weights (zero outside its own slab, its
+//     own pixel pair and the detector edge rule) into a tensor-memory row;
+//   * one thread issues two tcgen05.mma (M 128 voxels, N 128 rows, K 16
+//     pixels each) accumulating into the 128 x 128 FP32 tile in tensor memory.
+// Weights carry the tilt's factor 2^(E0 - e(t)) (E0 the smallest exponent over
+// the tilts), so the accumulator counts in units of 2^-E0 for every tilt; the
+// store multiplies by the backprojection scale and 2^-E0.
+//
+// What decides which samples a voxel takes -- its detector coordinate, floor,
+// weight t, slab index and edge rule -- is the reference's float arithmetic,
+// bit for bit (as in gnc_bp.cu); the products and sums are FP16 x FP16 -> FP32
+// on the tensor cores.
+//
+// Warp roles (192 threads): warps 0-3 build weights and store the volume,
+// warp 4 issues the TMA loads, warp 5 owns the tensor memory and issues the
+// MMAs.  Stages: kSB shared-memory windows and kSA tensor-memory weight
+// buffers, each with a "full" and an "empty" mbarrier.  Every wait is bounded
+// and records a timeout in the plan's error word.
+#include <cuda.h>
+
+#include <cmath>
+#include <cstring>
+
+#include "gnc_common.cuh"
+
+namespace gnc {
+
+namespace {
+
+constexpr int kTX = 16, kTZ = 8;          // voxel tile (x, z): 128 voxels = M
+constexpr int kNR = 128;                  // Y rows per block = N
+constexpr int kKW = 32;                   // window pixels (two K = 16 steps)
+constexpr int kKMAX = 3;                  // slabs per tile and tilt
+constexpr int kSB = 4, kSA = 2;           // window stages, weight stages
+constexpr int kSlabBytes = kNR * kKW * 2;  // 8 KB: one slab's window
+constexpr int kStageBytes = kKMAX * kSlabBytes;
+constexpr int kACols = kKMAX * (kKW / 2);  // tensor-memory columns of one weight stage
+constexpr int kTmemCols = 256;            // 128 accumulator + 2 x 48 weight columns
+constexpr int kThreads = 192;
+constexpr unsigned kHintNs = 1000;
+
+constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+constexpr int kMagicBits = 0x4B400000;
+
+typedef unsigned long long u64;
+
+struct TcTilt {
+  int u0;      // first window pixel (multiple of 8; may be negative)
+  int k0, nk;  // first slab and slab count of the tile
+  float wfac;  // 2^(E0 - e(t))
+};
+
+constexpr size_t kSmemBytes = 1024 + (size_t)kSB * kStageBytes + (size_t)kTcMaxTilts * sizeof(TcTilt);
+
+__device__ __forceinline__ unsigned sa(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ float voxel_coordf(int i, int n) {
+  return (float)((double)i - 0.5 * (double)n + 0.5);
+}
+__device__ __forceinline__ float detector_coord(float xc, float zs, float off) {
+  return __fsub_rn(__fadd_rn(__fsub_rn(xc, zs), off), 0.5f);
+}
+__device__ __forceinline__ int floor_int(float q) {
+  return __float_as_int(__fadd_rd(q, kMagic)) - kMagicBits;
+}
+
+__device__ __forceinline__ void bar_init(u64 *b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(sa(b)), "r"(count));
+}
+__device__ __forceinline__ void bar_arrive(u64 *b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(sa(b)) : "memory");
+}
+__device__ __forceinline__ void bar_expect_tx(u64 *b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sa(b)), "r"(bytes)
+               : "memory");
+}
+// Bounded wait for the phase of the given parity; false (and the error word
+// set) if it did not complete within `limit` polls.
+__device__ __forceinline__ bool bar_wait(u64 *b, unsigned parity, unsigned limit, int *err) {
+  for (unsigned it = 0; it < limit; ++it) {
+    unsigned done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3; "
+        "selp.u32 %0, 1, 0, p; }"
+        : "=r"(done)
+        : "r"(sa(b)), "r"(parity), "r"(kHintNs)
+        : "memory");
+    if (done) return true;
+  }
+  if (err) atomicOr(err, 1);
+  return false;
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// Shared-memory operand descriptor: K-major, 64-byte swizzle, rows of 64
+// bytes in 8-row atoms of 512 bytes (stride between atoms 512 B).
+__device__ __forceinline__ u64 b_desc(unsigned addr) {
+  u64 d = (u64)((addr & 0x3FFFFu) >> 4);
+  d |= (u64)1 << 16;            // leading offset (unused for this layout)
+  d |= (u64)(512 >> 4) << 32;   // stride between 8-row atoms
+  d |= (u64)1 << 46;            // descriptor version
+  d |= (u64)4 << 61;            // 64-byte swizzle
+  return d;
+}
+// Instruction descriptor: FP16 A and B (K-major), FP32 D, M = 128, N = kNR.
+constexpr unsigned kIdesc = (1u << 4) | ((unsigned)(kNR >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void mma(unsigned d_tmem, unsigned a_tmem, u64 bdesc, unsigned acc) {
+  asm volatile(
+      "{ .reg .pred p; setp.ne.u32 p, %4, 0; "
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p; }" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(bdesc), "r"(kIdesc), "r"(acc));
+}
+__device__ __forceinline__ void mma_commit(u64 *b) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   sa(b))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_st16(unsigned taddr, const unsigned (&r)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15,%16};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld32(unsigned taddr, unsigned (&v)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+      "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
+        "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
+        "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kThreads, 2)
+k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
+  if (a.dyn) {
+    a.dscale = a.dyn[0];
+    a.doffset = a.dyn[1];
+  }
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ __align__(8) u64 full_b[kSB], empty_b[kSB], full_a[kSA], empty_a[kSA], done_bar;
+  __shared__ unsigned tmem_base;
+  __shared__ int s_e0;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const unsigned limit = a.wait_limit ? a.wait_limit : kBpWaitLimit;
+  // 1024-aligned windows (the 64-byte swizzle repeats every 512 bytes), then the tilt table
+  unsigned char *win = smem_raw + ((1024u - (sa(smem_raw) & 1023u)) & 1023u);
+  TcTilt *tab = (TcTilt *)(win + (size_t)kSB * kStageBytes);
+
+  const int ntx = (a.X + kTX - 1) / kTX;
+  const int x0 = (blockIdx.x % ntx) * kTX, z0 = (blockIdx.x / ntx) * kTZ;
+  const int y0 = blockIdx.y * kNR;
+
+  if (warp == 5) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     sa(&tmem_base)),
+                 "r"((unsigned)kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int i = 0; i < kSB; ++i) {
+      bar_init(&full_b[i], 1);
+      bar_init(&empty_b[i], 1);
+    }
+    for (int i = 0; i < kSA; ++i) {
+      bar_init(&full_a[i], 128);
+      bar_init(&empty_a[i], 1);
+    }
+    bar_init(&done_bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_e0 = 127;
+  }
+  __syncthreads();
+  // the tile's window and slabs per tilt: corners inside the volume (the
+  // coordinate and the slab index are monotone in x and in z)
+  const float cx0 = voxel_coordf(x0, a.X), cx1 = voxel_coordf(min(x0 + kTX, a.X) - 1, a.X);
+  const float cz0 = voxel_coordf(z0, a.Z), cz1 = voxel_coordf(min(z0 + kTZ, a.Z) - 1, a.Z);
+  for (int t = tid; t < a.T; t += kThreads) {
+    const TiltGeom g = a.geom[t];
+    const float off = a.offset[t];
+    const float xc0 = __fmul_rn(cx0, g.cos_a), xc1 = __fmul_rn(cx1, g.cos_a);
+    const float zs0 = __fmul_rn(cz0, g.sin_a), zs1 = __fmul_rn(cz1, g.sin_a);
+    const float q00 = detector_coord(xc0, zs0, off), q01 = detector_coord(xc0, zs1, off);
+    const float q10 = detector_coord(xc1, zs0, off), q11 = detector_coord(xc1, zs1, off);
+    const int p_lo = floor_int(fminf(fminf(q00, q01), fminf(q10, q11)));
+    int k_lo = 0, k_hi = 0;
+    if (a.D > 1) {
+      const int k00 = slab_index(cx0, cz0, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
+      const int k01 = slab_index(cx0, cz1, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
+      const int k10 = slab_index(cx1, cz0, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
+      const int k11 = slab_index(cx1, cz1, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
+      k_lo = min(min(k00, k01), min(k10, k11));
+      k_hi = max(max(k00, k01), max(k10, k11));
+    }
+    TcTilt tt;
+    tt.u0 = p_lo & ~7;  // round down to a multiple of 8 (also for negative p_lo)
+    tt.k0 = k_lo;
+    tt.nk = k_hi - k_lo + 1;
+    if (tt.nk > kKMAX) {  // excluded by backproject_tc_supported
+      tt.nk = kKMAX;
+      if (a.err) atomicOr(a.err, 2);
+    }
+    tt.wfac = 0.f;
+    tab[t] = tt;
+    atomicMin(&s_e0, (int)a.tilt_exp[t]);
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const int e0 = s_e0;
+  for (int t = tid; t < a.T; t += kThreads) tab[t].wfac = pow2f(max(-126, e0 - (int)a.tilt_exp[t]));
+  __syncthreads();
+  const unsigned tmem = tmem_base;
+
+  if (warp == 4) {
+    // ---- TMA producer
+    if (lane == 0) {
+      for (int i = 0; i < a.T; ++i) {
+        const int b = i % kSB;
+        bar_wait(&empty_b[b], ((i / kSB) & 1) ^ 1, limit, a.err);
+        const TcTilt tt = tab[i];
+        bar_expect_tx(&full_b[b], (unsigned)(tt.nk * kSlabBytes));
+        for (int s = 0; s < tt.nk; ++s) {
+          const unsigned dst = sa(win + (size_t)b * kStageBytes + (size_t)s * kSlabBytes);
+          const int plane = (tt.k0 + s) * a.T + i;
+          asm volatile(
+              "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes "
+              "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+              "l"(&map), "r"(tt.u0), "r"(y0), "r"(plane), "r"(sa(&full_b[b]))
+              : "memory");
+        }
+      }
+    }
+  } else if (warp == 5) {
+    // ---- MMA issuer
+    if (lane == 0) {
+      for (int i = 0; i < a.T; ++i) {
+        const int b = i % kSB, s_a = i % kSA;
+        bar_wait(&full_a[s_a], (i / kSA) & 1, limit, a.err);
+        bar_wait(&full_b[b], (i / kSB) & 1, limit, a.err);
+        tc_fence_after();
+        const int nk = tab[i].nk;
+        const unsigned wbase = sa(win + (size_t)b * kStageBytes);
+        for (int s = 0; s < nk; ++s)
+          for (int kk = 0; kk < 2; ++kk)
+            mma(tmem, tmem + kNR + s_a * kACols + s * (kKW / 2) + kk * 8,
+                b_desc(wbase + s * kSlabBytes + kk * 32), (i | s | kk) != 0 ? 1u : 0u);
+        mma_commit(&empty_a[s_a]);
+        mma_commit(&empty_b[b]);
+      }
+      mma_commit(&done_bar);
+    }
+  } else {
+    // ---- weight builders: thread m = voxel (x0 + m % 16, z0 + m / 16) = tensor-memory lane m
+    const int m = tid;
+    const int x = x0 + (m & (kTX - 1)), z = z0 + (m >> 4);
+    const bool inside = x < a.X && z < a.Z;
+    const float xf = voxel_coordf(x, a.X), zf = voxel_coordf(z, a.Z);
+    const unsigned lane_addr = (unsigned)(warp * 32) << 16;
+    for (int i = 0; i < a.T; ++i) {
+      const int s_a = i % kSA;
+      bar_wait(&empty_a[s_a], ((i / kSA) & 1) ^ 1, limit, a.err);
+      tc_fence_after();
+      const TcTilt tt = tab[i];
+      const TiltGeom g = a.geom[i];
+      const float q = detector_coord(__fmul_rn(xf, g.cos_a), __fmul_rn(zf, g.sin_a), a.offset[i]);
+      const float r = __fadd_rd(q, kMagic);
+      const int fl = __float_as_int(r) - kMagicBits;
+      const float tw = __fsub_rn(q, __fsub_rn(r, kMagic));
+      const int k = tt.nk > 1 ? slab_index(xf, zf, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D)
+                              : tt.k0;
+      const int pos = fl - tt.u0;
+      // the reference skips samples unless 0 <= floor <= N - 2
+      bool valid = inside && fl >= 0 && fl <= a.N - 2;
+      if (valid && (pos < 0 || pos > kKW - 2)) {  // excluded by the tile's window
+        valid = false;
+        if (a.err) atomicOr(a.err, 4);
+      }
+      const unsigned h0 = __half_as_ushort(__float2half_rn(__fmul_rn(__fsub_rn(1.f, tw), tt.wfac)));
+      const unsigned h1 = __half_as_ushort(__float2half_rn(__fmul_rn(tw, tt.wfac)));
+      const u64 pair = (u64)(h0 | (h1 << 16)) << ((pos & 1) * 16);
+      const unsigned lo = (unsigned)pair, hi = (unsigned)(pair >> 32);
+      const int idx = pos >> 1;
+#pragma unroll
+      for (int s = 0; s < kKMAX; ++s) {
+        if (s < tt.nk) {
+          const bool mine = valid && (k - tt.k0 == s);
+          unsigned w[16];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) w[j] = !mine ? 0u : (j == idx ? lo : (j == idx + 1 ? hi : 0u));
+          tmem_st16(tmem + lane_addr + kNR + s_a * kACols + s * (kKW / 2), w);
+        }
+      }
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+      tc_fence_before();
+      bar_arrive(&full_a[s_a]);
+    }
+    // ---- store: the accumulator of voxel m, rows y0 .. y0 + 127
+    bar_wait(&done_bar, 0, limit, a.err);
+    tc_fence_after();
+    const float sc = a.geom[0].scale * pow2f(max(-126, min(127, -e0)));
+#pragma unroll 1
+    for (int c = 0; c < kNR; c += 32) {
+      unsigned v[32];
+      tmem_ld32(tmem + lane_addr + (unsigned)c, v);
+      if (inside) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int y = y0 + c + j;
+          if (y < a.Y) a.vol[((size_t)y * a.Z + z) * a.X + x] = __uint_as_float(v[j]) * sc;
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 5)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"((unsigned)kTmemCols));
+}
+
+// One block per tilt: the sum of squares of the tilt's input (double), then its
+// F16T exponent.
+__global__ void k_tilt_exponents(const float *__restrict__ in, size_t per_tilt, int t0,
+                                 const float *__restrict__ factor, double gain,
+                                 int8_t *__restrict__ exp) {
+  const int t = t0 + blockIdx.x;
+  const float *p = in + (size_t)t * per_tilt;
+  double acc = 0.0;
+  const bool vec = (((uintptr_t)p) & 15) == 0 && per_tilt % 4 == 0;
+  if (vec) {
+    const float4 *p4 = (const float4 *)p;
+    for (size_t i = threadIdx.x; i < per_tilt / 4; i += blockDim.x) {
+      const float4 v = __ldg(p4 + i);
+      acc += (double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z + (double)v.w * v.w;
+    }
+  } else {
+    for (size_t i = threadIdx.x; i < per_tilt; i += blockDim.x) {
+      const double v = p[i];
+      acc += v * v;
+    }
+  }
+  __shared__ double part[32];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += part[w];
+    exp[t] = (int8_t)f16t_exponent(s, factor ? factor[t] : 1.0f, gain);
+  }
+}
+
+cudaError_t launch_tilt_exponents(const float *input, size_t per_tilt, int t0, int nt,
+                                  const float *factor, double gain, int8_t *exp, cudaStream_t s) {
+  if (nt <= 0) return cudaSuccess;
+  k_tilt_exponents<<<nt, 1024, 0, s>>>(input, per_tilt, t0, factor, gain, exp);
+  return cudaGetLastError();
+}
+
+bool backproject_tc_supported(int N, int T, float dscale, int D, bool uniform_centre) {
+  if (!uniform_centre || N % 8 != 0 || N < 2 || T < 1 || T > kTcMaxTilts) return false;
+  if (D <= 1) return true;
+  // a 16 x 8 tile spans at most sqrt(16^2 + 8^2) pixels in height; slabs are
+  // 1 / dscale pixels thick
+  const double span = std::sqrt((double)kTX * kTX + (double)kTZ * kTZ) + 2.0;
+  return (int)std::ceil(span * std::fabs((double)dscale)) + 1 <= kKMAX;
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+cudaError_t make_tc_map(const void *staged, int D, int T, int H, int N, TcMap *out) {
+  static_assert(sizeof(CUtensorMap) == sizeof(TcMap), "tensor map size");
+  static EncodeTiledFn encode = nullptr;
+  if (!encode) {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                     cudaEnableDefault, &q);
+    if (e != cudaSuccess) return e;
+    if (!fn || q != cudaDriverEntryPointSuccess) return cudaErrorNotSupported;
+    encode = (EncodeTiledFn)fn;
+  }
+  // rows (D T, H, N) of FP16; box: 32 pixels x kNR rows x 1 (64-byte rows, swizzled)
+  cuuint64_t dims[3] = {(cuuint64_t)N, (cuuint64_t)H, (cuuint64_t)D * T};
+  cuuint64_t strides[2] = {(cuuint64_t)N * 2, (cuuint64_t)H * N * 2};
+  cuuint32_t box[3] = {(cuuint32_t)kKW, (cuuint32_t)kNR, 1};
+  cuuint32_t es[3] = {1, 1, 1};
+  CUtensorMap m;
+  std::memset(&m, 0, sizeof m);
+  const CUresult r = encode(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, const_cast<void *>(staged),
+                            dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                            CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+  std::memcpy(out->bytes, &m, sizeof m);
+  return cudaSuccess;
+}
+
+cudaError_t launch_backproject_tc(const BpArgs &a, const TcMap &map, cudaStream_t s) {
+  if (cudaError_t e = ensure_dynamic_smem<k_bp_tc>((int)kSmemBytes)) return e;
+  const int ntx = (a.X + kTX - 1) / kTX, ntz = (a.Z + kTZ - 1) / kTZ;
+  dim3 grid(ntx * ntz, (a.Y + kNR - 1) / kNR);
+  CUtensorMap m;
+  std::memcpy(&m, map.bytes, sizeof m);
+  k_bp_tc<<<grid, kThreads, kSmemBytes, s>>>(a, m);
+  return cudaGetLastError();
+}
+
+}  // namespace gnc

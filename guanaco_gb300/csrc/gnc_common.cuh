@@ -24,7 +24,7 @@ bool fft_length_supported(long n);
 bool make_fft_factors(int n, FftPlan *out);
 
 // ---- staging element types ------------------------------------------------
-enum Staging : int { kStageF32 = 0, kStageF16 = 1 };
+enum Staging : int { kStageF32 = 0, kStageF16 = 1, kStageF16T = 2 };
 
 // One staged detector pixel n of a row pair (rows a = 2 y2, b = 2 y2 + 1):
 //   F32: float2 (v_a, v_b)                                              8 bytes
@@ -43,6 +43,24 @@ __device__ __forceinline__ uint2 staged_record_f16(float2 v0, float2 v1) {
   r.y = *(const unsigned *)&dv;
   return r;
 }
+
+// F16T staging (the tensor-core backprojector): plain FP16 rows (D, T, H, N),
+// row y of slab d and tilt t at ((d T + t) H + y) N, every value of tilt t
+// multiplied by 2^e(t) with one exponent per tilt (int8, T).  e(t) comes from
+// a bound on every filtered value of the tilt: |factor_t| * gain * ||input_t||_2
+// (gain = H W for the unnormalised CTF correction, 1 otherwise; the phase flip
+// and the ramp filter do not increase the L2 norm, and no value of a vector
+// exceeds its L2 norm), brought just below 2^14, so no value overflows FP16
+// and the largest keeps full precision unless the bound is more than 2^16 loose.
+__host__ __device__ __forceinline__ int f16t_exponent(double norm2, float factor, double gain) {
+  const double b = fabs((double)factor) * gain * sqrt(norm2);
+  if (!(b > 0.0) || !(b < 1e300)) return 0;  // zero, NaN or inf: nothing to scale
+  int ex = 0;
+  frexp(b, &ex);  // b = m 2^ex, m in [0.5, 1): b 2^(14 - ex) < 2^14
+  const int e = 14 - ex;
+  return e < -100 ? -100 : (e > 100 ? 100 : e);
+}
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }
 
 // Per-tilt backprojection geometry, computed on the host with the reference's
 // float arithmetic (src/libguanaco/reconstructor.cpp:35-47).
@@ -132,9 +150,10 @@ struct RowStageArgs {
   const float *tilt_factor;
   // output
   int out_staged;        // 1: staged pairs (Y2, D, T, N), 0: plain rows
-  int staging;           // kStageF32 / kStageF16 when out_staged
-  void *staged;          // float2 pairs or FP16 records
+  int staging;           // kStageF32 / kStageF16 / kStageF16T when out_staged
+  void *staged;          // float2 pairs, FP16 records, or F16T rows
   int8_t *row_exp;       // (Y2, D, T, 2) FP16 exponents when staging == F16
+  const int8_t *tilt_exp;  // (T) exponents e(t) when staging == F16T
   float *out_rows;       // plain rows: (nt, D, H, N) at [t][d][y][n]
   const int2 *live;      // per tilt (first, last) slab the volume reads; others are
                          // skipped (staged output only), or null: all slabs
@@ -148,6 +167,13 @@ cudaError_t launch_row_stage(const RowStageArgs &a, cudaStream_t s);
 template <auto KERNEL>
 inline cudaError_t ensure_dynamic_smem(int bytes) {
   return cudaFuncSetAttribute(KERNEL, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+// F16T: row y of slab d and tilt t in the staged stack, and the tilt's scale.
+__device__ __forceinline__ __half *f16t_row(const RowStageArgs &a, int d, int t, int y) {
+  return (__half *)a.staged + (((size_t)d * a.T + t) * a.H + y) * (size_t)a.N;
+}
+__device__ __forceinline__ float f16t_scale(const RowStageArgs &a, int t) {
+  return __int_as_float((127 + (int)a.tilt_exp[t]) << 23);
 }
 // Row pairs a row-stage launch covers: rows 2 y2_begin .. of every (tilt, slab).
 __host__ __device__ inline int row_pairs(const RowStageArgs &a) {
@@ -169,6 +195,9 @@ struct BpArgs {
   const float *dyn;       // device (dscale, doffset) overriding the two above, or null
   unsigned wait_limit;    // polls before a bulk-copy wait gives up (0: kBpWaitLimit)
   unsigned wait_probe;    // test hook, 0 = off: see gnc_debug_wait_probe
+  const int8_t *tilt_exp; // F16T: (T) per-tilt exponents (staged = F16T rows)
+  int y_begin;            // F16T: stack row of this launch's first volume row
+  int stack_h;            // F16T: rows of each (slab, tilt) plane of the staged stack
 };
 // Default poll limit of the backprojector's bounded mbarrier waits (each poll
 // suspends for at most about 2 us, so about 2 s in all).
@@ -186,6 +215,24 @@ cudaError_t launch_slab_map(const BpArgs &a, int32_t *out, cudaStream_t s);
 // the slab index is monotone in x and in z, so the extremes lie at the
 // volume's corners (the same float expression as the backprojectors).
 cudaError_t launch_live_slabs(const BpArgs &a, int2 *live, cudaStream_t s);
+
+// ---- tensor-core backprojection of F16T rows (gnc_bp_tc.cu) -----------------
+// Whether the tensor-core kernel takes this geometry (shared centre, width a
+// multiple of 8, at most kTcMaxTilts tilts, at most kTcMaxSlabs slabs per tile).
+constexpr int kTcMaxTilts = 512;
+bool backproject_tc_supported(int N, int T, float dscale, int D, bool uniform_centre);
+// The TMA descriptor of F16T rows at `staged` for (D, T, H, N); 128 bytes,
+// passed to the kernel by value.
+struct TcMap {
+  alignas(64) unsigned char bytes[128];
+};
+cudaError_t make_tc_map(const void *staged, int D, int T, int H, int N, TcMap *out);
+cudaError_t launch_backproject_tc(const BpArgs &a, const TcMap &map, cudaStream_t s);
+// Per-tilt F16T exponents of the input (T tilts of `per_tilt` floats, tilts
+// [t0, t0 + nt)): exp[t] = f16t_exponent(||input_t||^2, factor[t], gain).
+cudaError_t launch_tilt_exponents(const float *input, size_t per_tilt, int t0, int nt,
+                                  const float *factor, double gain, int8_t *exp,
+                                  cudaStream_t s);
 
 // Single-slice backprojection of plain filtered rows (D, T, N) into (Z, X):
 // the per-call path of guanaco.detail.recon.

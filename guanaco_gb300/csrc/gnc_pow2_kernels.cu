@@ -290,6 +290,18 @@ __global__ void __launch_bounds__(256) k_row_p2(RowStageArgs a, const float2 *__
 #pragma unroll
       for (int m = 0; m < 16; ++m) dst[j + m * P::NT] = yv[m];
     }
+  } else if (STAGED && F16 && a.staging == kStageF16T) {
+    // plain FP16 rows scaled by the tilt's 2^e(t) (the branch is uniform: no
+    // barrier below is skipped by part of the block)
+    if (active) {
+      const float sc = f16t_scale(a, t);
+      __half *da = f16t_row(a, d, t, ya);
+#pragma unroll
+      for (int m = 0; m < 16; ++m) {
+        da[j + m * P::NT] = __float2half_rn(yv[m].x * sc);
+        if (hb) da[N + j + m * P::NT] = __float2half_rn(yv[m].y * sc);
+      }
+    }
   } else if (STAGED && F16) {
     // the records need pixel n + 1, held by another thread: exchange the
     // group's row pair through its (no longer needed) transform buffer
@@ -421,7 +433,7 @@ static cudaError_t row_p2(const RowStageArgs &a, cudaStream_t s) {
 template <int N>
 static cudaError_t row_p2_dispatch(const RowStageArgs &a, cudaStream_t s) {
   const bool sp = a.input_spectra != 0, rm = a.ramp != 0, st = a.out_staged != 0;
-  const bool h = a.staging == kStageF16;
+  const bool h = a.staging != kStageF32;
   if (sp && rm && st && !h) return row_p2<N, true, true, true, false>(a, s);
   if (sp && rm && st && h) return row_p2<N, true, true, true, true>(a, s);
   if (!sp && rm && st && !h) return row_p2<N, false, true, true, false>(a, s);

@@ -118,6 +118,16 @@ __global__ void k_row_stage(RowStageArgs a, FftPlan planN, FftPlan plan2N, int r
         if (RAMP) v = make_float2(v.x / out_scale, v.y / out_scale);
         dst[n] = make_float2(v.x * f, v.y * f);
       }
+    } else if (STAGED && F16 && a.staging == kStageF16T) {
+      // plain FP16 rows scaled by the tilt's 2^e(t)
+      const float sc = f16t_scale(a, t);
+      __half *da = f16t_row(a, d, t, ya);
+      for (int n = threadIdx.x; n < N; n += blockDim.x) {
+        float2 v = row[n];
+        if (RAMP) v = make_float2(v.x / out_scale, v.y / out_scale);
+        da[n] = __float2half_rn(v.x * f * sc);
+        if (hb) da[N + n] = __float2half_rn(v.y * f * sc);
+      }
     } else if (STAGED && F16) {
       float ma = 0.f, mb = 0.f;
       for (int n = threadIdx.x; n < N; n += blockDim.x) {
@@ -194,7 +204,7 @@ cudaError_t launch_row_stage(const RowStageArgs &a, cudaStream_t s) {
   if (a.N == 128 || a.N == 256 || a.N == 384 || a.N == 512) return launch_row_stage_w512(a, s);
   if (pow2_fast(a.N)) return launch_row_stage_p2(a, s);
   const bool sp = a.input_spectra != 0, rm = a.ramp != 0, st = a.out_staged != 0;
-  const bool h = a.staging == kStageF16;
+  const bool h = a.staging != kStageF32;
   if (sp && rm && st && !h) return launch_variant<true, true, true, false>(a, s);
   if (sp && rm && st && h) return launch_variant<true, true, true, true>(a, s);
   if (!sp && rm && st && !h) return launch_variant<false, true, true, false>(a, s);

@@ -302,6 +302,15 @@ __global__ void __launch_bounds__(128, 3) k_row_w1024(RowStageArgs a,
     float2 *dst = (float2 *)a.staged + (((size_t)y2 * a.D + d) * a.T + t) * kN;
 #pragma unroll
     for (int m = 0; m < 32; ++m) dst[32 * m + lane] = y[m];
+  } else if (STAGED && F16 && a.staging == kStageF16T) {
+    // plain FP16 rows scaled by the tilt's 2^e(t)
+    const float sc = f16t_scale(a, t);
+    __half *da = f16t_row(a, d, t, ya);
+#pragma unroll
+    for (int m = 0; m < 32; ++m) {
+      da[32 * m + lane] = __float2half_rn(y[m].x * sc);
+      if (hb) da[kN + 32 * m + lane] = __float2half_rn(y[m].y * sc);
+    }
   } else if (STAGED && F16) {
     float ma = 0.f, mb = 0.f;
 #pragma unroll
@@ -399,7 +408,7 @@ static cudaError_t row_w1024(const RowStageArgs &a, cudaStream_t s) {
 
 cudaError_t launch_row_stage_w1024(const RowStageArgs &a, cudaStream_t s) {
   const bool sp = a.input_spectra != 0, rm = a.ramp != 0, st = a.out_staged != 0;
-  const bool h = a.staging == kStageF16;
+  const bool h = a.staging != kStageF32;
   if (sp && rm && st && !h) return row_w1024<true, true, true, false>(a, s);
   if (sp && rm && st && h) return row_w1024<true, true, true, true>(a, s);
   if (!sp && rm && st && !h) return row_w1024<false, true, true, false>(a, s);

@@ -238,6 +238,17 @@ __global__ void __launch_bounds__(128) k_row_w512(RowStageArgs a, const float2 *
 #pragma unroll
       for (int m = 0; m < 16; ++m) dst[l + L * m] = yv[m];
     }
+  } else if (STAGED && F16 && a.staging == kStageF16T) {
+    // plain FP16 rows scaled by the tilt's 2^e(t)
+    if (active) {
+      const float sc = f16t_scale(a, t);
+      __half *da = f16t_row(a, d, t, ya);
+#pragma unroll
+      for (int m = 0; m < 16; ++m) {
+        da[l + L * m] = __float2half_rn(yv[m].x * sc);
+        if (hb) da[N + l + L * m] = __float2half_rn(yv[m].y * sc);
+      }
+    }
   } else if (STAGED && F16) {
     float ma = 0.f, mb = 0.f;
 #pragma unroll
@@ -344,7 +355,7 @@ static cudaError_t row_w512(const RowStageArgs &a, cudaStream_t s) {
 template <int N>
 static cudaError_t row_w512_dispatch(const RowStageArgs &a, cudaStream_t s) {
   const bool sp = a.input_spectra != 0, rm = a.ramp != 0, st = a.out_staged != 0;
-  const bool h = a.staging == kStageF16;
+  const bool h = a.staging != kStageF32;
   if (sp && rm && st && !h) return row_w512<N, true, true, true, false>(a, s);
   if (sp && rm && st && h) return row_w512<N, true, true, true, true>(a, s);
   if (!sp && rm && st && !h) return row_w512<N, false, true, true, false>(a, s);

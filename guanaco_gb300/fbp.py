@@ -93,7 +93,11 @@ class FbpDesc:
         d.weights = (None if self._weights is None
                      else self._weights.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
         d.minus = 1 if minus else 0
-        d.staging = _lib.GNC_STAGE_F16 if staging in ("f16", "fp16", "half") else _lib.GNC_STAGE_F32
+        stagings = {"f32": _lib.GNC_STAGE_F32, "f16": _lib.GNC_STAGE_F16,
+                    "f16t": _lib.GNC_STAGE_F16T}
+        if staging not in stagings:
+            raise ValueError(f"staging must be one of {sorted(stagings)}, not {staging!r}")
+        d.staging = stagings[staging]
         self.correcting = bool(d.correct)
         self.c = d
 

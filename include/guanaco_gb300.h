@@ -170,7 +170,13 @@ GNC_API int gnc_ctf_image_device(const gnc_ctf *c, int kind, const double *defoc
  * ---------------------------------------------------------------------- */
 typedef struct gnc_fbp_plan gnc_fbp_plan;
 
-enum { GNC_STAGE_F32 = 0, GNC_STAGE_F16 = 1 };
+/* Staging of the filtered rows between the ramp filter and the backprojection:
+ * F32; F16 (per-row exponents, CUDA-core backprojection); F16T (FP16 rows
+ * with one power-of-two scale per tilt, backprojected on the tensor cores
+ * with FP32 accumulation; where that kernel does not take the geometry --
+ * rows with different centres, a width not a multiple of 8, more than 512
+ * tilts or slabs thinner than about 10 pixels -- a plan uses F16). */
+enum { GNC_STAGE_F32 = 0, GNC_STAGE_F16 = 1, GNC_STAGE_F16T = 2 };
 enum { GNC_INPUT_RAW = 0, GNC_INPUT_CORRECTED = 1 };
 
 typedef struct {
@@ -196,7 +202,7 @@ typedef struct {
   double phase_shift_deg;
   const double *weights; /* host, T per-tilt weights (mp.py:135-141) or NULL */
   int minus;             /* transform == "minus" (mp.py:128-129) */
-  int staging;           /* GNC_STAGE_F32 or GNC_STAGE_F16 */
+  int staging;           /* GNC_STAGE_F32, GNC_STAGE_F16 or GNC_STAGE_F16T */
   double ctf_pixel_size; /* A, for the CTF only, in double as the reference's CTF
                             takes it (src/guanaco/detail/ext/ctf.h:142-149);
                             0 = pixel_size */
@@ -249,8 +255,8 @@ GNC_API int gnc_fbp_launches(const gnc_fbp_plan *plan);
 GNC_API int gnc_fbp_live_slabs(gnc_fbp_plan *plan, int32_t *h_out, void *stream);
 /* Which backprojection kernel gnc_fbp_execute runs for this plan: 0 the
  * exact kernel (rows with different centres, an odd detector width or too
- * many slabs per tile), else the fast kernel's slab capacity per tile (2 or 4);
- * -1 for a null plan. */
+ * many slabs per tile), 2 or 4 the CUDA-core fast kernel (its slab capacity
+ * per tile), 16 the tensor-core kernel of F16T staging; -1 for a null plan. */
 GNC_API int gnc_fbp_backprojector(const gnc_fbp_plan *plan);
 /* Test hook of the failure detection, no counterpart in the reference.
  * polls > 0: plans created afterwards (by gnc_fbp_plan_create and by the
@@ -271,7 +277,9 @@ GNC_API int gnc_fbp_check(gnc_fbp_plan *plan, void *stream);
  *   F32: float (v_a, v_b)
  *   F16: half (v_a, v_b, dv_a, dv_b), dv the difference of the next pixel's FP16
  *        value and this one (0 for the last pixel), value = half * 2^-e;
- *        with the (ceil(H/2), D, T, 2) int8 row exponents e. */
+ *        with the (ceil(H/2), D, T, 2) int8 row exponents e.
+ * F16T plans instead stage plain FP16 rows (D, T, H, W), value = half * 2^-e(t),
+ * with the (T) int8 tilt exponents in place of the row exponents. */
 GNC_API int gnc_fbp_staged(gnc_fbp_plan *plan, const void **d_staged, const int8_t **d_row_exp);
 
 /* ------------------------------------------------------------------------

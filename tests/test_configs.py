@@ -56,7 +56,7 @@ def _series(G, T, n, Z, blobs, seed, defocus=None, pixel_size=1.0):
     return ang, proj
 
 
-@pytest.mark.parametrize("staging", ["f32", "f16"])
+@pytest.mark.parametrize("staging", ["f32", "f16", "f16t"])
 def test_plain_fbp_256(G, oracle, staging):
     T, n, Z = 61, 256, 128
     ang, proj = _series(G, T, n, Z, 200, seed=0)
@@ -74,7 +74,7 @@ def test_plain_fbp_256(G, oracle, staging):
         assert rel_l2(vol, ref64) < FP16_TOL
 
 
-@pytest.mark.parametrize("staging", ["f32", "f16"])
+@pytest.mark.parametrize("staging", ["f32", "f16", "f16t"])
 def test_single_defocus_ctf_512(G, oracle, staging):
     T, n, Z, ps, df = 41, 512, 256, 1.35, 20000.0
     ang, proj = _series(G, T, n, Z, 500, seed=1, defocus=df, pixel_size=ps)
@@ -118,7 +118,7 @@ def series_3dctf(G, oracle):
     return ang, proj, desc, rows, ref32, ref64
 
 
-@pytest.mark.parametrize("staging", ["f32", "f16"])
+@pytest.mark.parametrize("staging", ["f32", "f16", "f16t"])
 def test_3dctf_ndf10_1024(G, series_3dctf, staging):
     ang, proj, desc, rows, ref32, ref64 = series_3dctf
     T, n = proj.shape[0], proj.shape[2]
@@ -161,7 +161,7 @@ def series_large_3dctf(request, G, oracle):
     return request.param, ang, proj, desc, rows, ref32, ref64
 
 
-@pytest.mark.parametrize("staging", ["f32", "f16"])
+@pytest.mark.parametrize("staging", ["f32", "f16", "f16t"])
 def test_large_3dctf_ndf20_4096_bands_vs_oracles(G, series_large_3dctf, staging):
     """BASELINE's large configuration (4096^2 at 0.8 A/px, 20 slabs, Z = 512):
     the 4096-point block transforms, the packed signs of 4096 rows and the

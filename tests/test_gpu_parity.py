@@ -3,7 +3,7 @@ golden vectors recorded from the reference.
 
 Tolerances (relative L2 over the whole output):
   * FP32 path vs the reference CPU path (golden / float oracle): 1e-4
-  * FP16-staged path vs the FP64 oracle: 1e-3
+  * FP16-staged paths (F16 records, F16T tensor-core rows) vs the FP64 oracle: 1e-3
   * slab indices and phase-flip signs: bit-exact
   * the exact backprojector given the oracle's filtered rows: bit-exact
 """
@@ -273,7 +273,7 @@ def _oracle_volume(oracle, proj, ang, c, ctf, mn, mx, Z, precision, weights=None
                           precision=precision)
 
 
-@pytest.mark.parametrize("staging", ["f32", "f16"])
+@pytest.mark.parametrize("staging", ["f32", "f16", "f16t"])
 @pytest.mark.parametrize("shape", [(17, 12, 48, 40, 5), (9, 7, 60, 30, 3), (21, 16, 64, 64, 1)])
 def test_pipeline_vs_oracles(torch, oracle, staging, shape):
     T, H, W, Z, D = shape
@@ -292,7 +292,7 @@ def test_pipeline_vs_oracles(torch, oracle, staging, shape):
 # runs them in chunks.  Tilts of very different magnitude per chunk change the
 # FP16 form's common exponent from chunk to chunk, so its accumulators are
 # rescaled at each chunk boundary.
-@pytest.mark.parametrize("staging", ["f32", "f16"])
+@pytest.mark.parametrize("staging", ["f32", "f16", "f16t"])
 def test_tilt_chunks_of_different_magnitude(torch, oracle, staging):
     T, H, W, Z, D = 300, 6, 48, 32, 3
     plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=T, H=H, W=W, Z=Z, D=D, staging=staging)
@@ -337,13 +337,69 @@ def test_fast_backprojector_tilt_chunks(torch, oracle, staging, D, variant):
     assert rel_l2(vol, exact.cpu().numpy()) < (1e-5 if staging == "f32" else 5e-4)
 
 
+# F16T staging: FP16 rows with one power-of-two scale per tilt, backprojected
+# on the tensor cores (tcgen05.mma, FP32 accumulation in tensor memory).  The
+# plan must pick that kernel, match the FP64 oracle within the FP16 tolerance
+# and the exact backprojector on the same FP16 rows closely (they differ only
+# in the FP16 interpolation weights and the summation order).  Shapes: volume
+# edges that cut tiles (X, Z not multiples of 16 and 8, rows not a multiple
+# of 128), several slabs per tile, one slab, 300 tilts, a 1024-pixel detector.
+@pytest.mark.parametrize("T,H,W,Z,X,D", [(17, 12, 48, 40, 48, 5), (9, 130, 64, 37, 64, 3),
+                                         (300, 6, 128, 48, 128, 3), (21, 16, 64, 64, 64, 1),
+                                         (13, 4, 1024, 300, 1024, 10), (11, 20, 96, 21, 53, 4)])
+def test_tensor_core_backprojector(torch, oracle, T, H, W, Z, X, D):
+    import guanaco_gb300 as G
+
+    rng = np.random.default_rng(T + W)
+    ang = np.deg2rad(np.linspace(-60, 60, T)).astype(np.float32)
+    c = G.get_centre((T, H, W), None, False)
+    df = 25000.0
+    mn, mx, step, nd = G.get_defocus_steps(df, D, None, W, c, 1.0)
+    plan = G.FbpPlan(T, H, W, ang, grid_height=Z, grid_width=X, centre=c, correct=True,
+                     num_defocus=nd, slab_defocus=G.api.slab_defoci(mn, nd, step),
+                     min_defocus=float(mn - df), max_defocus=float(mx - df), energy=300,
+                     spherical_aberration=2.7, staging="f16t")
+    assert plan.backprojector == 16
+    proj = rng.standard_normal((T, H, W)).astype(np.float32)
+    inp = dev(torch, proj)
+    vol = torch.empty(plan.volume_shape, dtype=torch.float32, device="cuda")
+    ref = torch.empty_like(vol)
+    plan.stage(inp)
+    plan.backproject(vol, exact=False)
+    plan.backproject(ref, exact=True)
+    plan.check()
+    got = vol.cpu().numpy()
+    assert rel_l2(got, ref.cpu().numpy()) < 3e-4
+    if X == W:  # the oracle's volume is as wide as the detector
+        ctf = oracle.ctf_stack(W, H, 1.0, 300, mn, nd, step, 2.7)
+        want = oracle.fbp_ctf(proj, ang, c, 1.0, ctf, float(mn - df), float(mx - df), Z=Z,
+                              precision="f64")
+        assert rel_l2(got, want) < FP16_TOL
+    # the whole pipeline through the host-buffer entry point gives the same volume
+    np.testing.assert_array_equal(plan.execute_host(proj), got)
+
+
+def test_tensor_core_staging_falls_back(torch, oracle):
+    """Rows with different centres are outside the tensor-core kernel: an F16T
+    plan then stages FP16 records for the other backprojectors, within the
+    FP16 tolerance of the FP64 oracle."""
+    T, H, W, Z = 11, 6, 40, 30
+    centre = (W / 2 + np.linspace(-1.5, 2.0, H)).astype(np.float32)
+    plan, proj, ang, c, ctf, mn, mx = _plan_case(oracle, T=T, H=H, W=W, Z=Z, D=3, centre=centre,
+                                                 staging="f16t")
+    assert plan.backprojector == 0
+    vol = plan.execute_host(proj)
+    ref = _oracle_volume(oracle, proj, ang, c, ctf, mn, mx, Z, "f64")
+    assert rel_l2(vol, ref) < FP16_TOL
+
+
 # The host-buffer entry point overlaps its copies with the kernels (tilt groups
 # in, row slabs out; with CTF correction it filters row slab by row slab); it
 # must give exactly the device entry point's volume.  Shapes: power-of-two and
 # generic rows, an odd row count (a last slab with a single-row pair), and
 # 1024-pixel rows: three input groups of at least 8 MB and six volume slabs of
 # at least 16 MB, the last split in three.
-@pytest.mark.parametrize("staging", ["f32", "f16"])
+@pytest.mark.parametrize("staging", ["f32", "f16", "f16t"])
 @pytest.mark.parametrize("T,H,W,Z,D,ragged", [(37, 64, 256, 40, 4, False), (19, 90, 128, 30, 3, True),
                                                 (9, 22, 64, 48, 1, False), (11, 45, 256, 20, 2, False),
                                                 (5, 250, 128, 16, 2, False),
@@ -438,7 +494,7 @@ def test_linearity_at_full_detector_width(torch, oracle):
 
 
 # ------------------------------------------- power-of-two transform lengths
-@pytest.mark.parametrize("staging", ["f32", "f16"])
+@pytest.mark.parametrize("staging", ["f32", "f16", "f16t"])
 @pytest.mark.parametrize("shape", [(5, 256, 1024, 48, 3), (7, 512, 256, 64, 4),
                                    (3, 1024, 256, 32, 2), (6, 243, 512, 40, 5),
                                    (3, 2048, 256, 16, 2), (2, 4096, 128, 16, 3),
