@@ -247,11 +247,11 @@ def run_ours(args, rank, world, dist):
     clocks = ClockSampler(dev.index)
     clocks.start()
     res = {}
-    for form in (("f16", "f32") if large else ("f32", "f16")):
+    for form in (("f16", "f16t", "f32") if large else ("f32", "f16", "f16t")):
         res[form] = timed(form)
-        if large and form == "f16":  # one plan at a time in HBM at this size
-            plans.pop("f16").close()
-            vols.pop("f16")
+        if large and form != "f32":  # one plan at a time in HBM at this size
+            plans.pop(form).close()
+            vols.pop(form)
             torch.cuda.empty_cache()
     # end to end through the public host-buffer entry point: pinned input in,
     # volume out, every step
@@ -269,10 +269,11 @@ def run_ours(args, rank, world, dist):
     e2e_ms = (time.perf_counter() - t0) * 1e3
     clk = clocks.stop()
 
-    total32, total16, e2e_ms = reduce_max_over_ranks([res["f32"][0], res["f16"][0], e2e_ms],
-                                                     dist, dev)
+    total32, total16, total16t, e2e_ms = reduce_max_over_ranks(
+        [res["f32"][0], res["f16"][0], res["f16t"][0], e2e_ms], dist, dev)
     value32 = job_throughput(voxel_tilts(), args.steps, world, total32)
     value16 = job_throughput(voxel_tilts(), args.steps, world, total16)
+    value16t = job_throughput(voxel_tilts(), args.steps, world, total16t)
     e2e_value = job_throughput(voxel_tilts(), args.steps, world, e2e_ms)
 
     serving = run_serving(dev) if not args.no_serve else None
@@ -339,7 +340,13 @@ def run_ours(args, rank, world, dist):
                     "bp_ms": round(res["f32"][1], 4)},
             "f16": {"value": round(value16, 2), "ms_per_step": round(total16 / args.steps, 4),
                     "bp_ms": round(res["f16"][1], 4),
-                    "speedup_vs_f32": round(value16 / value32, 3)},
+                    "speedup_vs_f32": round(value16 / value32, 3),
+                    "staging": "FP16 records, per-row exponents, CUDA-core backprojection"},
+            "f16t": {"value": round(value16t, 2), "ms_per_step": round(total16t / args.steps, 4),
+                     "bp_ms": round(res["f16t"][1], 4),
+                     "speedup_vs_f32": round(value16t / value32, 3),
+                     "staging": ("FP16 rows, one power-of-two scale per tilt, tensor-core "
+                                 "backprojection (tcgen05, FP32 accumulation)")},
         },
         "e2e": {
             "value": round(e2e_value, 2), "unit": UNIT,
@@ -592,11 +599,13 @@ def oracle_sample(proj, vols):
 
     g32 = vols["f32"][sl].cpu().numpy()
     g16 = vols["f16"][sl].cpu().numpy()
+    g16t = vols["f16t"][sl].cpu().numpy()
     parity = {
         "rows_sampled": list(rows),
         "f32_vs_reference_cpu_rel_l2": rel(g32, r32),
         "f32_vs_fp64_oracle_rel_l2": rel(g32, r64),
         "f16_vs_fp64_oracle_rel_l2": rel(g16, r64),
+        "f16t_vs_fp64_oracle_rel_l2": rel(g16t, r64),
         "f32_max_abs_vs_fp64": float(np.abs(g32 - r64).max()),
         "reference_cpu_vs_fp64_rel_l2": rel(r32, r64),
     }
