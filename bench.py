@@ -499,8 +499,17 @@ def run_serving(dev):
         res = drive_stream(srv, stream, descs, inputs, pools, t_base)
         stats = srv.stats()
     lat = np.array([x[0] for x in res]) * 1e3
+    replay = np.array([bool(x[2]["graph"]) for x in res])
     span = max(x[2]["t_done"] for x in res) - t_base
     vt = sum(x[1] for x in res)
+
+    def pct(sel):
+        v = lat[sel]
+        if v.size == 0:
+            return {"requests": 0}
+        return {"requests": int(v.size), "p50_ms": round(float(np.percentile(v, 50)), 3),
+                "p99_ms": round(float(np.percentile(v, 99)), 3), "max_ms": round(float(v.max()), 3)}
+
     return {
         "workload": SERVE_NAME,
         "requests": len(res),
@@ -508,6 +517,8 @@ def run_serving(dev):
         "p99_ms": round(float(np.percentile(lat, 99)), 3),
         "max_ms": round(float(lat.max()), 3),
         "mean_ms": round(float(lat.mean()), 3),
+        "graph_replays_latency": pct(replay),
+        "direct_runs_latency": pct(~replay),
         "throughput_req_s": round(len(res) / span, 1),
         "value": round(vt / span / 1e9, 2),
         "unit": UNIT,

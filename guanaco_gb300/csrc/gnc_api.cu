@@ -197,6 +197,10 @@ struct gnc_fbp_plan {
   int *err = nullptr;        // device error word of the bounded waits
   unsigned wait_probe = 0;   // gnc_debug_wait_probe's value when the plan was created
   size_t bytes = 0;
+  // request-server plans: device memory from this pool, stream-ordered on
+  // alloc_stream (null: cudaMalloc / cudaFree)
+  cudaMemPool_t pool = nullptr;
+  cudaStream_t alloc_stream = nullptr;
   // host-buffer path (gnc_fbp_execute_host), created on its first call
   float *io_in = nullptr, *io_out = nullptr;
   float2 *gfull = nullptr;  // (T, D, H, W/2) flipped spectra (slab-major order)
@@ -205,23 +209,34 @@ struct gnc_fbp_plan {
   cudaEvent_t ev[kIoEvents] = {};
 };
 
+// Device memory of a plan: from cudaMalloc, or -- for plans of the request
+// server -- stream-ordered from the server's memory pool (no device-wide
+// synchronisation when it is allocated or freed).
+static void dfree(gnc_fbp_plan *p, void *ptr) {
+  if (!ptr) return;
+  if (p->pool)
+    cudaFreeAsync(ptr, p->alloc_stream);
+  else
+    cudaFree(ptr);
+}
+
 static void plan_free(gnc_fbp_plan *p) {
-  cudaFree(p->spec);
-  cudaFree(p->gbuf);
+  dfree(p, p->spec);
+  dfree(p, p->gbuf);
   if (p->ev_fork) cudaEventDestroy(p->ev_fork);
   for (cudaEvent_t e : p->ev_flip)
     if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : p->ev_rows)
     if (e) cudaEventDestroy(e);
   if (p->s_flip) cudaStreamDestroy(p->s_flip);
-  cudaFree(p->staged);
-  cudaFree(p->row_exp);
-  cudaFree(p->tilt_exp);
-  cudaFree(p->sign);
-  cudaFree(p->live);
-  cudaFree(p->params);
-  cudaFree(p->err);
-  cudaFree(p->io_in);
+  dfree(p, p->staged);
+  dfree(p, p->row_exp);
+  dfree(p, p->tilt_exp);
+  dfree(p, p->sign);
+  dfree(p, p->live);
+  dfree(p, p->params);
+  dfree(p, p->err);
+  cudaFree(p->io_in);  // the host-buffer path's buffers (never from the pool)
   cudaFree(p->io_out);
   cudaFree(p->gfull);
   for (cudaEvent_t e : p->ev)
@@ -234,6 +249,7 @@ template <typename T>
 static cudaError_t dalloc(gnc_fbp_plan *p, T **ptr, size_t count) {
   size_t b = std::max<size_t>(count, 1) * sizeof(T);
   p->bytes += b;
+  if (p->pool) return cudaMallocFromPoolAsync((void **)ptr, b, p->pool, p->alloc_stream);
   return cudaMalloc((void **)ptr, b);
 }
 
@@ -430,6 +446,18 @@ int *plan_error_word(gnc_fbp_plan *p) { return p->err; }
 
 }  // namespace gnc
 
+extern "C" {
+static int plan_create(const gnc_fbp_desc *d, cudaMemPool_t pool, cudaStream_t alloc,
+                       gnc_fbp_plan **out);
+}
+
+namespace gnc {
+int plan_create_pooled(const gnc_fbp_desc *d, cudaMemPool_t pool, cudaStream_t alloc,
+                       gnc_fbp_plan **out) {
+  return plan_create(d, pool, alloc, out);
+}
+}  // namespace gnc
+
 // ------------------------------------------------ shared request checks ---
 namespace gnc {
 
@@ -476,13 +504,18 @@ extern "C" {
 const char *gnc_last_error(void) { return last_error(); }
 int gnc_version(void) { return 100; }
 
-int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
+// pool / alloc: null for cudaMalloc'd plans, else the request server's pool and
+// the stream its allocations are ordered on
+static int plan_create(const gnc_fbp_desc *d, cudaMemPool_t pool, cudaStream_t alloc,
+                       gnc_fbp_plan **out) {
   GNC_REQUIRE(d != nullptr && out != nullptr);
   *out = nullptr;
   const int st = gnc::desc_check(d);
   if (st != GNC_OK) return st;
   const bool ctf = d->input == GNC_INPUT_RAW && d->correct;
   auto *p = new gnc_fbp_plan();
+  p->pool = pool;
+  p->alloc_stream = alloc;
   cudaGetDevice(&p->device);
   p->wait_probe = g_wait_probe.load();
   p->T = (int)d->num_angles;
@@ -512,7 +545,9 @@ int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
     p->offset = (float *)(p->params + p->pl.offset);
     std::vector<unsigned char> blk(p->pl.bytes, 0);
     fill_params(p, d, blk.data(), &p->uniform_centre, &p->dscale, &p->doffset, &p->sargs);
-    e = cudaMemcpy(p->params, blk.data(), blk.size(), cudaMemcpyHostToDevice);
+    // pageable source: the call returns once the bytes are staged
+    e = pool ? cudaMemcpyAsync(p->params, blk.data(), blk.size(), cudaMemcpyHostToDevice, alloc)
+             : cudaMemcpy(p->params, blk.data(), blk.size(), cudaMemcpyHostToDevice);
   }
   if (ctf) {
     size_t per_tilt = (size_t)p->D * p->H * half * sizeof(float2);
@@ -544,7 +579,8 @@ int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
       e = dalloc(p, &p->row_exp, (size_t)p->Y2 * p->D * p->T * 2);
   }
   if (e == cudaSuccess) e = dalloc(p, &p->err, 1);
-  if (e == cudaSuccess) e = cudaMemset(p->err, 0, sizeof(int));
+  if (e == cudaSuccess)
+    e = pool ? cudaMemsetAsync(p->err, 0, sizeof(int), alloc) : cudaMemset(p->err, 0, sizeof(int));
   if (e != cudaSuccess) {
     set_error(std::string("gnc_fbp_plan_create: ") + cudaGetErrorString(e));
     plan_free(p);
@@ -553,6 +589,10 @@ int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
   }
   *out = p;
   return GNC_OK;
+}
+
+int gnc_fbp_plan_create(const gnc_fbp_desc *d, gnc_fbp_plan **out) {
+  return plan_create(d, nullptr, nullptr, out);
 }
 
 int gnc_fbp_plan_destroy(gnc_fbp_plan *p) {

@@ -391,9 +391,10 @@ cudaError_t launch_tilt_exponents(const float *input, size_t per_tilt, int t0, i
 bool backproject_tc_supported(int N, int T, float dscale, int D, bool uniform_centre) {
   if (!uniform_centre || N % 8 != 0 || N < 2 || T < 1 || T > kTcMaxTilts) return false;
   if (D <= 1) return true;
-  // a 16 x 8 tile spans at most sqrt(16^2 + 8^2) pixels in height; slabs are
-  // 1 / dscale pixels thick
-  const double span = std::sqrt((double)kTX * kTX + (double)kTZ * kTZ) + 2.0;
+  // the voxel centres of a 16 x 8 tile span at most sqrt(15^2 + 7^2) pixels in
+  // height (plus one for rounding); slabs are 1 / dscale pixels thick
+  const double span =
+      std::sqrt((double)(kTX - 1) * (kTX - 1) + (double)(kTZ - 1) * (kTZ - 1)) + 1.0;
   return (int)std::ceil(span * std::fabs((double)dscale)) + 1 <= kKMAX;
 }
 

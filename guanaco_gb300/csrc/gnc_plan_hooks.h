@@ -22,5 +22,12 @@ int plan_set_request(gnc_fbp_plan *p, const gnc_fbp_desc *d, unsigned char *host
                      cudaStream_t s);
 // The plan's device error word (bounded waits that gave up).
 int *plan_error_word(gnc_fbp_plan *p);
+// gnc_fbp_plan_create with the plan's device memory allocated from `pool`,
+// ordered on stream `alloc` (cudaMallocFromPoolAsync; freed with
+// cudaFreeAsync on the same stream when the plan is destroyed, so neither
+// synchronises the device).  Its buffers may be used on another stream once
+// `alloc` has been synchronised (or waited on with an event).
+int plan_create_pooled(const gnc_fbp_desc *d, cudaMemPool_t pool, cudaStream_t alloc,
+                       gnc_fbp_plan **out);
 
 }  // namespace gnc

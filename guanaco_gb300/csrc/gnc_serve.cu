@@ -22,6 +22,14 @@
 // plans), up to kLookAhead younger requests may pass it, at most kMaxSkips
 // times in a row, after which the scheduler waits for memory to free up.
 //
+// Memory: plans and request buffers come from a CUDA memory pool of the
+// server (stream-ordered cudaMallocFromPoolAsync / cudaFreeAsync on the
+// builder's stream, the pool keeping up to the budget reserved), and the
+// page-locked parameter blocks of released plans are kept for reuse, so
+// creating and releasing plans while requests run neither synchronises the
+// device (as cudaMalloc, cudaFree and cudaFreeHost do) nor copies
+// synchronously.
+//
 // Locking: gn_server::mu guards the queue, the request table, the slots'
 // state, the cache bookkeeping and the statistics.  No CUDA call is made while
 // it is held (a host callback waiting for it would otherwise hold up a device
@@ -51,6 +59,7 @@ struct Cached {
   gnc_fbp_plan *plan = nullptr;
   float *d_in = nullptr, *d_out = nullptr;
   unsigned char *h_params = nullptr;  // page-locked parameter block
+  size_t h_bytes = 0;                  // its size
   cudaGraphExec_t exec = nullptr;
   size_t bytes = 0;
   bool busy = false;
@@ -107,7 +116,10 @@ struct gnc_server {
   uint64_t next_id = 1, tick = 0;
   int head_skips = 0;
   std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
-  cudaStream_t s_cap = nullptr;
+  cudaStream_t s_cap = nullptr;  // the builder's stream: captures, pool allocations and frees
+  cudaMemPool_t pool = nullptr;
+  std::mutex host_mu;  // page-locked parameter blocks for reuse: (bytes, pointer)
+  std::vector<std::pair<size_t, unsigned char *>> host_blocks;
   gnc_server_stats st{};
 
   double now() const {
@@ -127,12 +139,43 @@ void CUDART_CB on_done(void *arg) {
   S->cv_sched.notify_one();
 }
 
-void release(Cached *c) {  // CUDA frees: call without the lock
+// Without the lock, on the builder thread (or at destruction): the plan's
+// memory goes back to the pool on the builder's stream (its last use on a
+// slot has finished: only idle plans are released), its page-locked block to
+// the reuse list.
+void release(gnc_server *S, Cached *c) {
   if (c->exec) cudaGraphExecDestroy(c->exec);
   if (c->plan) gnc_fbp_plan_destroy(c->plan);
-  cudaFree(c->d_in);
-  cudaFree(c->d_out);
-  if (c->h_params) cudaFreeHost(c->h_params);
+  if (c->d_in) cudaFreeAsync(c->d_in, S->s_cap);
+  if (c->d_out) cudaFreeAsync(c->d_out, S->s_cap);
+  if (c->h_params) {
+    std::lock_guard<std::mutex> lk(S->host_mu);
+    S->host_blocks.emplace_back(c->h_bytes, c->h_params);
+  }
+  c->exec = nullptr;
+  c->plan = nullptr;
+  c->d_in = c->d_out = nullptr;
+  c->h_params = nullptr;
+}
+
+// A page-locked block of at least `bytes` (a released one of up to twice the
+// size when there is one); its size in *got.
+unsigned char *host_block(gnc_server *S, size_t bytes, size_t *got) {
+  {
+    std::lock_guard<std::mutex> lk(S->host_mu);
+    for (size_t i = 0; i < S->host_blocks.size(); ++i)
+      if (S->host_blocks[i].first >= bytes && S->host_blocks[i].first <= 2 * bytes + 4096) {
+        unsigned char *p = S->host_blocks[i].second;
+        *got = S->host_blocks[i].first;
+        S->host_blocks.erase(S->host_blocks.begin() + i);
+        return p;
+      }
+  }
+  unsigned char *p = nullptr;
+  const size_t rounded = (bytes + 4095) & ~(size_t)4095;
+  if (cudaHostAlloc((void **)&p, rounded, cudaHostAllocDefault) != cudaSuccess) return nullptr;
+  *got = rounded;
+  return p;
 }
 
 Cached *find_idle(gnc_server *S, const std::string &key) {
@@ -188,14 +231,22 @@ void fail(gnc_server *S, Request *r, int status, const std::string &msg) {
   S->st.failed++;
 }
 
-// Without the lock: plan, buffers and parameter block of a new cache entry.
-int create_entry(Cached *c, const Request *r) {
-  int st = gnc_fbp_plan_create(&r->desc, &c->plan);
+// Without the lock, on the builder thread: plan, buffers and parameter block
+// of a new cache entry, from the pool on the builder's stream; ready for use
+// on any stream when this returns.
+int create_entry(gnc_server *S, Cached *c, const Request *r) {
+  int st = gnc::plan_create_pooled(&r->desc, S->pool, S->s_cap, &c->plan);
   if (st != GNC_OK) return st;
-  cudaError_t e = cudaMalloc((void **)&c->d_in, r->in_bytes);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&c->d_out, r->out_bytes);
+  cudaError_t e = cudaMallocFromPoolAsync((void **)&c->d_in, r->in_bytes, S->pool, S->s_cap);
   if (e == cudaSuccess)
-    e = cudaHostAlloc((void **)&c->h_params, gnc::plan_param_bytes(c->plan), cudaHostAllocDefault);
+    e = cudaMallocFromPoolAsync((void **)&c->d_out, r->out_bytes, S->pool, S->s_cap);
+  if (e == cudaSuccess) {
+    c->h_params = host_block(S, gnc::plan_param_bytes(c->plan), &c->h_bytes);
+    if (!c->h_params) e = cudaErrorMemoryAllocation;
+  }
+  // the allocations and the plan's parameter upload are ordered on the
+  // builder's stream; the slots' streams use them after this
+  if (e == cudaSuccess) e = cudaStreamSynchronize(S->s_cap);
   if (e != cudaSuccess) {
     gnc::set_error(std::string("gnc_server: ") + cudaGetErrorString(e));
     return e == cudaErrorMemoryAllocation ? GNC_ERR_OUT_OF_MEMORY : GNC_ERR_CUDA;
@@ -350,16 +401,16 @@ void build_loop(gnc_server *S) {
     gnc_server::Build b = std::move(S->builds.front());
     S->builds.pop_front();
     lk.unlock();
-    for (auto &v : b.victims) release(v.get());
+    for (auto &v : b.victims) release(S, v.get());
     b.victims.clear();
     std::string msg;
-    int st = create_entry(b.c, b.r);
+    int st = create_entry(S, b.c, b.r);
     if (st != GNC_OK) msg = gnc::last_error();
     if (st == GNC_OK) {
       st = enqueue(S, b.sl, b.r, b.c, true);
       if (st != GNC_OK) msg = gnc::last_error();
     }
-    if (st != GNC_OK) release(b.c);
+    if (st != GNC_OK) release(S, b.c);
     lk.lock();
     if (st != GNC_OK) {
       S->used -= b.c->bytes;
@@ -423,6 +474,19 @@ int gnc_server_create(size_t budget_bytes, int slots, gnc_server **server) {
   S->budget = budget_bytes;
   S->slots.resize(slots);
   cudaError_t e = cudaStreamCreateWithFlags(&S->s_cap, cudaStreamNonBlocking);
+  if (e == cudaSuccess) {
+    // the plans' pool: keeps what is freed (up to the budget) instead of
+    // returning it to the driver, so later plans are carved from it
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = S->device;
+    e = cudaMemPoolCreate(&S->pool, &props);
+    if (e == cudaSuccess) {
+      unsigned long long keep = (unsigned long long)budget_bytes;
+      e = cudaMemPoolSetAttribute(S->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  }
   for (Slot &sl : S->slots) {
     sl.srv = S.get();
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sl.s, cudaStreamNonBlocking);
@@ -435,6 +499,7 @@ int gnc_server_create(size_t budget_bytes, int slots, gnc_server **server) {
       if (sl.h_err) cudaFreeHost(sl.h_err);
     }
     if (S->s_cap) cudaStreamDestroy(S->s_cap);
+    if (S->pool) cudaMemPoolDestroy(S->pool);
     return GNC_ERR_CUDA;
   }
   S->st.budget_bytes = budget_bytes;
@@ -466,7 +531,10 @@ int gnc_server_destroy(gnc_server *S) {
   S->th_build.join();
   cudaSetDevice(S->device);
   for (Slot &sl : S->slots) cudaStreamSynchronize(sl.s);
-  for (auto &c : S->cache) release(c.get());
+  for (auto &c : S->cache) release(S, c.get());
+  cudaStreamSynchronize(S->s_cap);  // the pool's frees
+  for (auto &hb : S->host_blocks) cudaFreeHost(hb.second);
+  if (S->pool) cudaMemPoolDestroy(S->pool);
   for (Slot &sl : S->slots) {
     cudaStreamDestroy(sl.s);
     cudaFreeHost(sl.h_err);

@@ -344,7 +344,8 @@ def test_fast_backprojector_tilt_chunks(torch, oracle, staging, D, variant):
 # in the FP16 interpolation weights and the summation order).  Shapes: volume
 # edges that cut tiles (X, Z not multiples of 16 and 8, rows not a multiple
 # of 128), several slabs per tile, one slab, 300 tilts, a 1024-pixel detector.
-@pytest.mark.parametrize("T,H,W,Z,X,D", [(17, 12, 48, 40, 48, 5), (9, 130, 64, 37, 64, 3),
+@pytest.mark.parametrize("T,H,W,Z,X,D", [(17, 12, 48, 40, 48, 5), (17, 12, 64, 40, 64, 6),
+                                         (9, 130, 64, 37, 64, 3),
                                          (300, 6, 128, 48, 128, 3), (21, 16, 64, 64, 64, 1),
                                          (13, 4, 1024, 300, 1024, 10), (11, 20, 96, 21, 53, 4)])
 def test_tensor_core_backprojector(torch, oracle, T, H, W, Z, X, D):

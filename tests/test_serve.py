@@ -51,17 +51,27 @@ def _alone(G, args, kw, proj):
 # (size, tilts, ndf, staging): repeated shapes replay a captured graph
 MIX = [(64, 11, 3, "f32"), (128, 21, 5, "f16"), (96, 9, 1, "f32"), (64, 11, 3, "f32"),
        (128, 15, 4, "f32"), (64, 11, 3, "f16"), (128, 21, 5, "f16"), (96, 9, 1, "f32"),
-       (64, 11, 3, "f32"), (160, 13, 2, "f16"), (128, 15, 4, "f32"), (64, 11, 3, "f32")]
+       (64, 11, 3, "f32"), (160, 13, 2, "f16"), (128, 15, 4, "f32"), (64, 11, 3, "f32"),
+       (128, 13, 3, "f16t"), (128, 13, 3, "f16t")]
+
+# The sizes and parameter ranges of the benchmark's serving stream (256^2,
+# 384^2 and 512^2 projections through the 1024-pixel-class register
+# transforms, 31-61 tilts, up to ten slabs, FP32, FP16 and F16T staging).
+MIX_LARGE = [(256, 31, 7, "f32"), (384, 41, 10, "f16"), (512, 31, 4, "f16t"),
+             (256, 31, 7, "f32"), (512, 61, 10, "f32"), (384, 41, 10, "f16t"),
+             (256, 41, 2, "f16"), (512, 31, 4, "f16t"), (384, 31, 1, "f32"),
+             (256, 31, 7, "f32")]
 
 
-def test_served_results_equal_alone(G):
+@pytest.mark.parametrize("mix,slots", [(MIX, 4), (MIX_LARGE, 6)], ids=["small", "large"])
+def test_served_results_equal_alone(G, mix, slots):
     from guanaco_gb300 import serve
 
     reqs = []
-    for i, (n, T, D, st) in enumerate(MIX):
+    for i, (n, T, D, st) in enumerate(mix):
         args, kw, proj = _request(G, n, T, D, st, seed=i, df=15000.0 + 2500.0 * i)
         reqs.append((args, kw, proj, _alone(G, args, kw, proj)))
-    with serve.Server(budget_bytes=8 << 30, slots=4) as srv:
+    with serve.Server(budget_bytes=16 << 30, slots=slots) as srv:
         ids, outs = [], []
         for args, kw, proj, _ in reqs:  # all in flight together
             desc = G.FbpDesc(*args, **kw)
@@ -77,10 +87,10 @@ def test_served_results_equal_alone(G):
         assert info["status"] == 0 and not info["device_error"]
         assert info["t_submit"] <= info["t_start"] <= info["t_done"]
         np.testing.assert_array_equal(got, want)
-    assert stats["completed"] == len(MIX) and stats["failed"] == 0
+    assert stats["completed"] == len(mix) and stats["failed"] == 0
     assert stats["graph_launches"] > 0          # repeated shapes replayed their graph
     assert stats["peak_in_flight"] > 1          # requests overlapped on the device
-    assert stats["plans_created"] < len(MIX)    # shapes shared plans
+    assert stats["plans_created"] < len(mix)    # shapes shared plans
 
 
 def test_budget_admission_releases_idle_plans(G):
