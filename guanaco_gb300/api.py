@@ -188,8 +188,12 @@ def reconstruct(tomogram, angles, reconstruction=None, centre=None, pixel_size=1
     stack in one pass instead of one ``recon`` call per row.
 
     Accepts (THETA, Y, X), (Y, THETA, X), (THETA, D, Y, X) or (Y, D, THETA, X)
-    as the reference does; returns the (Y, X, X) float32 volume.  ``ncore``,
-    ``nchunk`` and ``gpu_list`` only split the reference's Python loop and
+    as the reference does; returns the (Y, X, X) float32 volume.  With
+    ``gpu_list`` the Y rows are split into len(gpu_list) contiguous bands
+    (sizes as the reference's get_ncore_slices, mp.py:9-35) and band i runs on
+    device gpu_list[i], all bands at once (mp.py:61-66, 86-101): rows are
+    independent once the projections are corrected, so no exchange is needed.
+    ``ncore`` and ``nchunk`` only split the reference's per-row Python loop and
     are accepted and ignored."""
     _gpu(device)
     t = np.asarray(tomogram)
@@ -208,17 +212,48 @@ def reconstruct(tomogram, angles, reconstruction=None, centre=None, pixel_size=1
         assert reconstruction.shape[2] == W, "Inconsistent reconstruction/sinogram shape"
     centre = get_centre((H, T, W), centre)
     weights = get_weights(np.asarray(angles), angular_weights)
-    plan = FbpPlan(T, H, W, angles, grid_height=W, grid_width=W, centre=centre,
-                   pixel_size=pixel_size, input="corrected" if t.ndim == 4 else "raw",
-                   correct=False, num_defocus=D, min_defocus=min_defocus,
-                   max_defocus=max_defocus, weights=weights, minus=(transform == "minus"),
-                   staging=staging)
-    try:
-        vol = plan.execute_host(t)
-    finally:
-        plan.close()
-    reconstruction[...] = vol
+
+    def run_band(y0, y1):
+        band = np.ascontiguousarray(t[..., y0:y1, :])
+        plan = FbpPlan(T, y1 - y0, W, angles, grid_height=W, grid_width=W,
+                       centre=centre[y0:y1], pixel_size=pixel_size,
+                       input="corrected" if t.ndim == 4 else "raw", correct=False,
+                       num_defocus=D, min_defocus=min_defocus, max_defocus=max_defocus,
+                       weights=weights, minus=(transform == "minus"), staging=staging)
+        try:
+            reconstruction[y0:y1] = plan.execute_host(band)
+        finally:
+            plan.close()
+
+    if not gpu_list:
+        run_band(0, H)
+        return reconstruction
+    bands = row_bands(H, len(gpu_list))
+    import concurrent.futures as cf
+
+    import torch
+
+    def worker(gpu, y0, y1):
+        torch.cuda.set_device(int(gpu))  # this thread's current device
+        run_band(y0, y1)
+
+    with cf.ThreadPoolExecutor(len(bands)) as ex:
+        for f in [ex.submit(worker, g, y0, y1) for g, (y0, y1) in zip(gpu_list, bands)
+                  if y1 > y0]:
+            f.result()
     return reconstruction
+
+
+def row_bands(nrows, nbands):
+    """Contiguous row bands of sizes nrows // nbands, the first nrows % nbands
+    one row larger (get_ncore_slices, src/guanaco/detail/mp.py:9-35)."""
+    size, extra = divmod(int(nrows), int(nbands))
+    bands, y0 = [], 0
+    for i in range(int(nbands)):
+        y1 = y0 + size + (1 if i < extra else 0)
+        bands.append((y0, y1))
+        y0 = y1
+    return bands
 
 
 def reconstruct_ctf(projections, angles, centre=None, pixel_size=1, energy=300, defocus=None,

@@ -63,3 +63,18 @@ def test_public_functions_refuse_the_cpu_path():
         G.reconstruct(proj, np.zeros(3, np.float32), device="cpu")
     with pytest.raises(RuntimeError, match="device path only"):
         G.correct_projections(proj, device="cpu")
+
+
+def test_row_bands_split_like_the_reference():
+    """The gpu_list split of api.reconstruct: contiguous bands with the
+    leftover rows on the first bands (mp.py:9-35)."""
+    from guanaco_gb300 import api
+
+    assert api.row_bands(10, 3) == [(0, 4), (4, 7), (7, 10)]
+    assert api.row_bands(4, 4) == [(0, 1), (1, 2), (2, 3), (3, 4)]
+    assert api.row_bands(2, 3) == [(0, 1), (1, 2), (2, 2)]
+    for n, k in [(1024, 7), (5, 2), (0, 1)]:
+        b = api.row_bands(n, k)
+        assert b[0][0] == 0 and b[-1][1] == n
+        assert all(b[i][1] == b[i + 1][0] for i in range(k - 1))
+        assert max(y1 - y0 for y0, y1 in b) - min(y1 - y0 for y0, y1 in b) <= 1
