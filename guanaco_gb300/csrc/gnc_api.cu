@@ -181,6 +181,7 @@ struct gnc_fbp_plan {
   void *staged = nullptr;   // (Y2, D, T, W) pairs, or F16T rows (D, T, H, W)
   int8_t *row_exp = nullptr;
   int8_t *tilt_exp = nullptr;  // F16T: (T) per-tilt exponents
+  float *tilt_part = nullptr;  // F16T: (T, kTiltPartsMax) partial sums of squares
   TcMap tc_map{};              // F16T: TMA descriptor of the staged rows
   int8_t *sign = nullptr;   // (D, H, W/2 + 1)
   int2 *live = nullptr;     // (T): first and last slab the volume reads (CTF, D > 1)
@@ -232,6 +233,7 @@ static void plan_free(gnc_fbp_plan *p) {
   dfree(p, p->staged);
   dfree(p, p->row_exp);
   dfree(p, p->tilt_exp);
+  dfree(p, p->tilt_part);
   dfree(p, p->sign);
   dfree(p, p->live);
   dfree(p, p->params);
@@ -393,7 +395,7 @@ size_t plan_bytes(const gnc_fbp_desc *d) {
   }
   const int staging = effective_staging(d);
   if (staging == GNC_STAGE_F16T)
-    b += (D * T * H * W + 64) * 2 + T;
+    b += (D * T * H * W + 64) * 2 + T + T * kTiltPartsMax * sizeof(float);
   else
     b += (Y2 * D * T * W + 8) * kStagedPixelBytes;
   if (staging == GNC_STAGE_F16) b += Y2 * D * T * 2;
@@ -568,6 +570,7 @@ static int plan_create(const gnc_fbp_desc *d, cudaMemPool_t pool, cudaStream_t a
     const size_t elems = (size_t)p->D * p->T * p->H * p->W + 64;
     if (e == cudaSuccess) e = dalloc(p, (__half **)&p->staged, elems);
     if (e == cudaSuccess) e = dalloc(p, &p->tilt_exp, (size_t)p->T);
+    if (e == cudaSuccess) e = dalloc(p, &p->tilt_part, (size_t)p->T * kTiltPartsMax);
     if (e == cudaSuccess) e = make_tc_map(p->staged, p->D, p->T, p->H, p->W, &p->tc_map);
   } else {
     // +8 pixels: a 16-byte aligned bulk copy of the last row may run past its end
@@ -648,7 +651,8 @@ static cudaError_t tilt_exponents(gnc_fbp_plan *p, const float *input, int t0, i
   const size_t per_tilt = (size_t)(p->input == GNC_INPUT_CORRECTED ? p->D : 1) * p->H * p->W;
   // the unnormalised correction multiplies the L2 norm by at most H W
   const double gain = p->correct ? (double)p->H * p->W : 1.0;
-  return launch_tilt_exponents(input, per_tilt, t0, nt, p->tilt_factor, gain, p->tilt_exp, s);
+  return launch_tilt_exponents(input, per_tilt, t0, nt, p->tilt_factor, gain, p->tilt_part,
+                               p->tilt_exp, s);
 }
 
 // The staged-output arguments of the row stage.
@@ -932,7 +936,7 @@ int gnc_fbp_slab_map(gnc_fbp_plan *p, int32_t *d_out, void *stream) {
 
 int gnc_fbp_launches(const gnc_fbp_plan *p) {
   if (!p) return 0;
-  const int f16t = p->staging == GNC_STAGE_F16T ? 1 : 0;  // the per-tilt exponents
+  const int f16t = p->staging == GNC_STAGE_F16T ? 2 : 0;  // the per-tilt exponents
   if (!p->correct) return 2 + f16t;  // row stage, backprojection
   const int chunks = (p->T + p->chunk - 1) / p->chunk;
   // sign table (+ its packed copy, + the live slab ranges), row and column

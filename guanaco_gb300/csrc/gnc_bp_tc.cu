@@ -256,7 +256,7 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
           asm volatile(
               "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes "
               "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
-              "l"(&map), "r"(tt.u0), "r"(y0), "r"(plane), "r"(sa(&full_b[b]))
+              "l"(&map), "r"(tt.u0), "r"(a.y_begin + y0), "r"(plane), "r"(sa(&full_b[b]))
               : "memory");
         }
       }
@@ -349,42 +349,64 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
                  "r"((unsigned)kTmemCols));
 }
 
-// One block per tilt: the sum of squares of the tilt's input (double), then its
-// F16T exponent.
-__global__ void k_tilt_exponents(const float *__restrict__ in, size_t per_tilt, int t0,
-                                 const float *__restrict__ factor, double gain,
-                                 int8_t *__restrict__ exp) {
-  const int t = t0 + blockIdx.x;
+// Sum of squares of each input tilt in kTiltPartsMax partial sums (float: the
+// result only bounds the values to within a binade, and FP64 arithmetic is
+// slow on this GPU), then one thread per tilt turns them into the exponent.
+
+__global__ void k_tilt_sumsq(const float *__restrict__ in, size_t per_tilt, int t0,
+                             float *__restrict__ part) {
+  const int t = t0 + blockIdx.x, j = blockIdx.y;
   const float *p = in + (size_t)t * per_tilt;
-  double acc = 0.0;
-  const bool vec = (((uintptr_t)p) & 15) == 0 && per_tilt % 4 == 0;
+  const size_t chunk = (per_tilt + kTiltPartsMax - 1) / kTiltPartsMax;
+  const size_t b0 = (size_t)j * chunk, b1 = min(per_tilt, b0 + chunk);
+  float acc = 0.f;
+  size_t i = b0 + threadIdx.x;
+  // float4 loads over the 16-byte aligned middle of the chunk
+  const size_t a0 = min(b1, (b0 + 3) & ~(size_t)3);
+  const bool vec = ((((uintptr_t)p) & 15) == 0);
   if (vec) {
-    const float4 *p4 = (const float4 *)p;
-    for (size_t i = threadIdx.x; i < per_tilt / 4; i += blockDim.x) {
-      const float4 v = __ldg(p4 + i);
-      acc += (double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z + (double)v.w * v.w;
+    for (i = b0 + threadIdx.x; i < a0; i += blockDim.x) acc = fmaf(p[i], p[i], acc);
+    const float4 *p4 = (const float4 *)(p + a0);
+    const size_t n4 = (b1 - a0) / 4;
+    for (size_t k = threadIdx.x; k < n4; k += blockDim.x) {
+      const float4 v = __ldg(p4 + k);
+      acc = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, fmaf(v.w, v.w, acc))));
     }
+    for (i = a0 + 4 * n4 + threadIdx.x; i < b1; i += blockDim.x) acc = fmaf(p[i], p[i], acc);
   } else {
-    for (size_t i = threadIdx.x; i < per_tilt; i += blockDim.x) {
-      const double v = p[i];
-      acc += v * v;
-    }
+    for (; i < b1; i += blockDim.x) acc = fmaf(p[i], p[i], acc);
   }
-  __shared__ double part[32];
+  __shared__ float w_sum[32];
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  if ((threadIdx.x & 31) == 0) w_sum[threadIdx.x >> 5] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += part[w];
-    exp[t] = (int8_t)f16t_exponent(s, factor ? factor[t] : 1.0f, gain);
+    float s = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += w_sum[w];
+    part[(size_t)t * kTiltPartsMax + j] = s;
   }
 }
 
+__global__ void k_tilt_exp(const float *__restrict__ part, int t0, int nt,
+                           const float *__restrict__ factor, double gain,
+                           int8_t *__restrict__ exp) {
+  const int t = t0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= t0 + nt) return;
+  double s = 0.0;
+  for (int j = 0; j < kTiltPartsMax; ++j) s += (double)part[(size_t)t * kTiltPartsMax + j];
+  // float partial sums are within about 1e-4 of the exact sum: one part in
+  // 2^10 more keeps the bound above every value
+  exp[t] = (int8_t)f16t_exponent(s * (1.0 + 1.0 / 1024.0), factor ? factor[t] : 1.0f, gain);
+}
+
 cudaError_t launch_tilt_exponents(const float *input, size_t per_tilt, int t0, int nt,
-                                  const float *factor, double gain, int8_t *exp, cudaStream_t s) {
+                                  const float *factor, double gain, float *part, int8_t *exp,
+                                  cudaStream_t s) {
   if (nt <= 0) return cudaSuccess;
-  k_tilt_exponents<<<nt, 1024, 0, s>>>(input, per_tilt, t0, factor, gain, exp);
+  k_tilt_sumsq<<<dim3(nt, kTiltPartsMax), 512, 0, s>>>(input, per_tilt, t0, part);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_tilt_exp<<<(nt + 127) / 128, 128, 0, s>>>(part, t0, nt, factor, gain, exp);
   return cudaGetLastError();
 }
 

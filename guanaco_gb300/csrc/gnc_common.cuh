@@ -229,9 +229,11 @@ struct TcMap {
 cudaError_t make_tc_map(const void *staged, int D, int T, int H, int N, TcMap *out);
 cudaError_t launch_backproject_tc(const BpArgs &a, const TcMap &map, cudaStream_t s);
 // Per-tilt F16T exponents of the input (T tilts of `per_tilt` floats, tilts
-// [t0, t0 + nt)): exp[t] = f16t_exponent(||input_t||^2, factor[t], gain).
+// [t0, t0 + nt)): exp[t] = f16t_exponent(||input_t||^2, factor[t], gain);
+// `part` holds kTiltPartsMax floats per tilt of scratch.
+constexpr int kTiltPartsMax = 16;
 cudaError_t launch_tilt_exponents(const float *input, size_t per_tilt, int t0, int nt,
-                                  const float *factor, double gain, int8_t *exp,
+                                  const float *factor, double gain, float *part, int8_t *exp,
                                   cudaStream_t s);
 
 // Single-slice backprojection of plain filtered rows (D, T, N) into (Z, X):
