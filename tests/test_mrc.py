@@ -76,3 +76,43 @@ def test_rejects_non_mrc(tmp_path):
     p.write_bytes(b"\0" * 2048)
     with pytest.raises(ValueError):
         mrc.open_mrc(str(p))
+
+
+def test_fixture_written_from_the_specification(tmp_path):
+    """A file written byte by byte from the MRC2014 specification and the FEI1
+    record layout (tests/golden/make_mrc_fixture.py, independent of this
+    module): read back field by field, and the same stack written by this
+    module gives the same bytes wherever the format fixes them."""
+    import os
+    import sys
+
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    import make_mrc_fixture as fx
+
+    path = os.path.join(os.path.dirname(__file__), "golden", "mrc2014_fei1_stack.mrc")
+    with mrc.open_mrc(path) as f:
+        np.testing.assert_array_equal(f.data, fx.data())
+        assert f.data.shape == (fx.T, fx.NY, fx.NX)
+        assert f.voxel_size["x"] == pytest.approx(fx.PIXEL, rel=1e-6)
+        assert f.voxel_size["y"] == pytest.approx(fx.PIXEL, rel=1e-6)
+        np.testing.assert_array_equal(mrc.fei1_angles_deg(f), fx.TILTS)
+        assert np.all(f.extended_header["Defocus"] == fx.DEFOCUS)
+        assert int(f.header["nversion"]) == 20140 and int(f.header["ispg"]) == 0
+    want = open(path, "rb").read()
+    out = str(tmp_path / "written.mrc")
+    with mrc.new_mrc(out, (fx.T, fx.NY, fx.NX), np.float32, voxel_size=fx.PIXEL,
+                     fei1=True) as f:
+        f.data[...] = fx.data()
+        f.extended_header["Alpha tilt"] = fx.TILTS
+        f.extended_header["Defocus"] = fx.DEFOCUS
+        f.extended_header["Metadata version"] = 2
+    got = open(out, "rb").read()
+    assert len(got) == len(want)
+    # every header word the format fixes (all but the labels; statistics equal
+    # to float32 rounding), then the extended header and the data, exactly
+    fixed = [(0, 76), (88, 96), (104, 112), (196, 220)]
+    for a, b in fixed:
+        assert got[a:b] == want[a:b], (a, b)
+    np.testing.assert_allclose(np.frombuffer(got[76:88], "<f4"), np.frombuffer(want[76:88], "<f4"),
+                               rtol=1e-6)
+    assert got[1024:] == want[1024:]
