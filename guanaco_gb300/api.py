@@ -190,9 +190,10 @@ def reconstruct(tomogram, angles, reconstruction=None, centre=None, pixel_size=1
     Accepts (THETA, Y, X), (Y, THETA, X), (THETA, D, Y, X) or (Y, D, THETA, X)
     as the reference does; returns the (Y, X, X) float32 volume.  With
     ``gpu_list`` the Y rows are split into len(gpu_list) contiguous bands
-    (sizes as the reference's get_ncore_slices, mp.py:9-35) and band i runs on
-    device gpu_list[i], all bands at once (mp.py:61-66, 86-101): rows are
-    independent once the projections are corrected, so no exchange is needed.
+    (sizes as the reference's get_ncore_slices, mp.py:9-35, each edge moved to
+    the next even row) and band i runs on device gpu_list[i], all bands at
+    once (mp.py:61-66, 86-101): rows are independent once the projections are
+    corrected, so no exchange is needed.
     ``ncore`` and ``nchunk`` only split the reference's per-row Python loop and
     are accepted and ignored."""
     _gpu(device)
@@ -228,7 +229,9 @@ def reconstruct(tomogram, angles, reconstruction=None, centre=None, pixel_size=1
     if not gpu_list:
         run_band(0, H)
         return reconstruction
-    bands = row_bands(H, len(gpu_list))
+    # band edges on even rows: the filter transforms rows in pairs, so a pair
+    # never straddles two bands and the volume is the unsplit one bit for bit
+    bands = [(min(H, y0 + (y0 & 1)), min(H, y1 + (y1 & 1))) for y0, y1 in row_bands(H, len(gpu_list))]
     import concurrent.futures as cf
 
     import torch

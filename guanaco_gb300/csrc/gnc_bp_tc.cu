@@ -6,16 +6,17 @@
 // (two non-zeros per voxel: (1 - t) at the voxel's pixel floor(p), t at the
 // next one, src/libguanaco/reconstructor.cpp:76-86) and the staged rows.  A
 // block owns 128 voxels -- a 16 (x) by 8 (z) tile, compact so that for any
-// tilt they project onto at most 18 detector pixels -- and 128 Y rows.  Per
+// tilt they project onto at most 18 detector pixels -- and 256 Y rows.  Per
 // tilt and per defocus slab the tile reaches:
-//   * one TMA load brings the 32-pixel window [u0, u0 + 32) of the 128 rows
+//   * one TMA load brings the 32-pixel window [u0, u0 + 32) of the 256 rows
 //     (u0 a multiple of 8) into shared memory, 64-byte swizzled;
-//   * the 128 builder threads (one per voxel) compute the voxel's detector
-//     coordinate, floor, weight and slab with the reference's float
-//     operations, and store its 32 weights (zero outside its own slab, its
-//     own pixel pair and the detector edge rule) into a tensor-memory row;
-//   * one thread issues two tcgen05.mma (M 128 voxels, N 128 rows, K 16
-//     pixels each) accumulating into the 128 x 128 FP32 tile in tensor memory.
+//   * 256 builder threads (two per voxel, one per half of the window) compute
+//     the voxel's detector coordinate, floor, weight and slab with the
+//     reference's float operations, and store its 32 weights (zero outside
+//     its own slab, its own pixel pair and the detector edge rule) into a
+//     tensor-memory row;
+//   * one thread issues two tcgen05.mma (M 128 voxels, N 256 rows, K 16
+//     pixels each) accumulating into the 128 x 256 FP32 tile in tensor memory.
 // Weights carry the tilt's factor 2^(E0 - e(t)) (E0 the smallest exponent over
 // the tilts), so the accumulator counts in units of 2^-E0 for every tilt; the
 // store multiplies by the backprojection scale and 2^-E0.
@@ -25,11 +26,14 @@
 // bit for bit (as in gnc_bp.cu); the products and sums are FP16 x FP16 -> FP32
 // on the tensor cores.
 //
-// Warp roles (192 threads): warps 0-3 build weights and store the volume,
-// warp 4 issues the TMA loads, warp 5 owns the tensor memory and issues the
-// MMAs.  Stages: kSB shared-memory windows and kSA tensor-memory weight
-// buffers, each with a "full" and an "empty" mbarrier.  Every wait is bounded
-// and records a timeout in the plan's error word.
+// Warp roles (320 threads, one block per SM): warps 0-7 build weights
+// (warps w and w + 4 the two window halves of voxels 32 (w % 4) ..) and store
+// the volume, warp 8 issues the TMA loads, warp 9 owns the tensor memory and
+// issues the MMAs.  Stages: kSB shared-memory windows and kSA tensor-memory
+// weight buffers, each with a "full" and an "empty" mbarrier; the builders
+// compute a tilt's weights before they wait for its buffer, and read the
+// tilt's geometry from a shared-memory table filled once per block.  Every
+// wait is bounded and records a timeout in the plan's error word.
 #include <cuda.h>
 
 #include <cmath>
@@ -42,15 +46,16 @@ namespace gnc {
 namespace {
 
 constexpr int kTX = 16, kTZ = 8;          // voxel tile (x, z): 128 voxels = M
-constexpr int kNR = 128;                  // Y rows per block = N
+constexpr int kNR = 256;                  // Y rows per block = N
 constexpr int kKW = 32;                   // window pixels (two K = 16 steps)
 constexpr int kKMAX = 3;                  // slabs per tile and tilt
-constexpr int kSB = 4, kSA = 2;           // window stages, weight stages
-constexpr int kSlabBytes = kNR * kKW * 2;  // 8 KB: one slab's window
+constexpr int kSB = 3, kSA = 4;           // window stages, weight stages
+constexpr int kSlabBytes = kNR * kKW * 2;  // 16 KB: one slab's window
 constexpr int kStageBytes = kKMAX * kSlabBytes;
 constexpr int kACols = kKMAX * (kKW / 2);  // tensor-memory columns of one weight stage
-constexpr int kTmemCols = 256;            // 128 accumulator + 2 x 48 weight columns
-constexpr int kThreads = 192;
+constexpr int kTmemCols = 512;            // 256 accumulator + 4 x 48 weight columns
+constexpr int kBuilders = 256;            // warps 0-7
+constexpr int kThreads = kBuilders + 64;  // + TMA warp + MMA warp
 constexpr unsigned kHintNs = 1000;
 
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
@@ -62,6 +67,8 @@ struct TcTilt {
   int u0;      // first window pixel (multiple of 8; may be negative)
   int k0, nk;  // first slab and slab count of the tile
   float wfac;  // 2^(E0 - e(t))
+  float cos_a, sin_a, off;  // the tilt's geometry (reconstructor.cpp:35-47)
+  float pad;
 };
 
 constexpr size_t kSmemBytes = 1024 + (size_t)kSB * kStageBytes + (size_t)kTcMaxTilts * sizeof(TcTilt);
@@ -146,6 +153,12 @@ __device__ __forceinline__ void tmem_st16(unsigned taddr, const unsigned (&r)[16
       "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
       : "memory");
 }
+__device__ __forceinline__ void tmem_st8(unsigned taddr, const unsigned (&r)[8]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])
+      : "memory");
+}
 __device__ __forceinline__ void tmem_ld32(unsigned taddr, unsigned (&v)[32]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
@@ -161,7 +174,7 @@ __device__ __forceinline__ void tmem_ld32(unsigned taddr, unsigned (&v)[32]) {
 
 }  // namespace
 
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, 1)
 k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
   if (a.dyn) {
     a.dscale = a.dyn[0];
@@ -181,7 +194,7 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
   const int x0 = (blockIdx.x % ntx) * kTX, z0 = (blockIdx.x / ntx) * kTZ;
   const int y0 = blockIdx.y * kNR;
 
-  if (warp == 5) {
+  if (warp == 9) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      sa(&tmem_base)),
                  "r"((unsigned)kTmemCols));
@@ -193,7 +206,7 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
       bar_init(&empty_b[i], 1);
     }
     for (int i = 0; i < kSA; ++i) {
-      bar_init(&full_a[i], 128);
+      bar_init(&full_a[i], kBuilders);
       bar_init(&empty_a[i], 1);
     }
     bar_init(&done_bar, 1);
@@ -231,6 +244,10 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
       if (a.err) atomicOr(a.err, 2);
     }
     tt.wfac = 0.f;
+    tt.cos_a = g.cos_a;
+    tt.sin_a = g.sin_a;
+    tt.off = off;
+    tt.pad = 0.f;
     tab[t] = tt;
     atomicMin(&s_e0, (int)a.tilt_exp[t]);
   }
@@ -242,7 +259,7 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
   __syncthreads();
   const unsigned tmem = tmem_base;
 
-  if (warp == 4) {
+  if (warp == 8) {
     // ---- TMA producer
     if (lane == 0) {
       for (int i = 0; i < a.T; ++i) {
@@ -261,7 +278,7 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
         }
       }
     }
-  } else if (warp == 5) {
+  } else if (warp == 9) {
     // ---- MMA issuer
     if (lane == 0) {
       for (int i = 0; i < a.T; ++i) {
@@ -281,23 +298,22 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
       mma_commit(&done_bar);
     }
   } else {
-    // ---- weight builders: thread m = voxel (x0 + m % 16, z0 + m / 16) = tensor-memory lane m
-    const int m = tid;
+    // ---- weight builders: voxel m = (x0 + m % 16, z0 + m / 16) = tensor-memory
+    // lane m; this thread writes the window half h (pixels 16 h .. 16 h + 15,
+    // columns 8 h .. 8 h + 7 of each slab's block)
+    const int m = 32 * (warp & 3) + lane, h = warp >> 2;
     const int x = x0 + (m & (kTX - 1)), z = z0 + (m >> 4);
     const bool inside = x < a.X && z < a.Z;
     const float xf = voxel_coordf(x, a.X), zf = voxel_coordf(z, a.Z);
-    const unsigned lane_addr = (unsigned)(warp * 32) << 16;
+    const unsigned lane_addr = (unsigned)(32 * (warp & 3)) << 16;
     for (int i = 0; i < a.T; ++i) {
       const int s_a = i % kSA;
-      bar_wait(&empty_a[s_a], ((i / kSA) & 1) ^ 1, limit, a.err);
-      tc_fence_after();
       const TcTilt tt = tab[i];
-      const TiltGeom g = a.geom[i];
-      const float q = detector_coord(__fmul_rn(xf, g.cos_a), __fmul_rn(zf, g.sin_a), a.offset[i]);
+      const float q = detector_coord(__fmul_rn(xf, tt.cos_a), __fmul_rn(zf, tt.sin_a), tt.off);
       const float r = __fadd_rd(q, kMagic);
       const int fl = __float_as_int(r) - kMagicBits;
       const float tw = __fsub_rn(q, __fsub_rn(r, kMagic));
-      const int k = tt.nk > 1 ? slab_index(xf, zf, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D)
+      const int k = tt.nk > 1 ? slab_index(xf, zf, tt.sin_a, tt.cos_a, a.dscale, a.doffset, a.D)
                               : tt.k0;
       const int pos = fl - tt.u0;
       // the reference skips samples unless 0 <= floor <= N - 2
@@ -310,27 +326,31 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
       const unsigned h1 = __half_as_ushort(__float2half_rn(__fmul_rn(tw, tt.wfac)));
       const u64 pair = (u64)(h0 | (h1 << 16)) << ((pos & 1) * 16);
       const unsigned lo = (unsigned)pair, hi = (unsigned)(pair >> 32);
-      const int idx = pos >> 1;
+      const int idx = (pos >> 1) - 8 * h;  // word of this half holding the pixel pair
+      // the weights first, then the wait for the buffer: the arithmetic above
+      // overlaps the MMAs still reading it
+      bar_wait(&empty_a[s_a], ((i / kSA) & 1) ^ 1, limit, a.err);
+      tc_fence_after();
 #pragma unroll
       for (int s = 0; s < kKMAX; ++s) {
         if (s < tt.nk) {
           const bool mine = valid && (k - tt.k0 == s);
-          unsigned w[16];
+          unsigned w[8];
 #pragma unroll
-          for (int j = 0; j < 16; ++j) w[j] = !mine ? 0u : (j == idx ? lo : (j == idx + 1 ? hi : 0u));
-          tmem_st16(tmem + lane_addr + kNR + s_a * kACols + s * (kKW / 2), w);
+          for (int j = 0; j < 8; ++j) w[j] = !mine ? 0u : (j == idx ? lo : (j == idx + 1 ? hi : 0u));
+          tmem_st8(tmem + lane_addr + kNR + s_a * kACols + s * (kKW / 2) + 8 * h, w);
         }
       }
       asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       tc_fence_before();
       bar_arrive(&full_a[s_a]);
     }
-    // ---- store: the accumulator of voxel m, rows y0 .. y0 + 127
+    // ---- store: the accumulator of voxel m; this thread's half of the rows
     bar_wait(&done_bar, 0, limit, a.err);
     tc_fence_after();
     const float sc = a.geom[0].scale * pow2f(max(-126, min(127, -e0)));
 #pragma unroll 1
-    for (int c = 0; c < kNR; c += 32) {
+    for (int c = h * (kNR / 2); c < (h + 1) * (kNR / 2); c += 32) {
       unsigned v[32];
       tmem_ld32(tmem + lane_addr + (unsigned)c, v);
       if (inside) {
@@ -344,7 +364,7 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 5)
+  if (warp == 9)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"((unsigned)kTmemCols));
 }
