@@ -29,10 +29,12 @@
 // Warp roles (320 threads, one block per SM): warps 0-7 build weights
 // (warps w and w + 4 the two window halves of voxels 32 (w % 4) ..) and store
 // the volume, warp 8 issues the TMA loads, warp 9 owns the tensor memory and
-// issues the MMAs.  Stages: kSB shared-memory windows and kSA tensor-memory
-// weight buffers, each with a "full" and an "empty" mbarrier; the builders
-// compute a tilt's weights before they wait for its buffer, and read the
-// tilt's geometry from a shared-memory table filled once per block.  Every
+// issues the MMAs.  A ring of kSB shared-memory window slots (a tilt takes
+// one per slab it reaches, mostly one) and kSA tensor-memory weight stages,
+// each with a "full" and an "empty" mbarrier; the windows of the tilt
+// kPrefetch ahead are prefetched into L2, so the loads find them there.  The
+// builders compute a tilt's weights before they wait for its buffer, and read
+// the tilt's geometry from a shared-memory table filled once per block.  Every
 // wait is bounded and records a timeout in the plan's error word.
 #include <cuda.h>
 
@@ -49,9 +51,9 @@ constexpr int kTX = 16, kTZ = 8;          // voxel tile (x, z): 128 voxels = M
 constexpr int kNR = 256;                  // Y rows per block = N
 constexpr int kKW = 32;                   // window pixels (two K = 16 steps)
 constexpr int kKMAX = 3;                  // slabs per tile and tilt
-constexpr int kSB = 3, kSA = 4;           // window stages, weight stages
+constexpr int kSB = 8, kSA = 4;           // window slots (one slab each), weight stages
+constexpr int kPrefetch = 8;              // tilts whose windows are prefetched into L2 ahead
 constexpr int kSlabBytes = kNR * kKW * 2;  // 16 KB: one slab's window
-constexpr int kStageBytes = kKMAX * kSlabBytes;
 constexpr int kACols = kKMAX * (kKW / 2);  // tensor-memory columns of one weight stage
 constexpr int kTmemCols = 512;            // 256 accumulator + 4 x 48 weight columns
 constexpr int kBuilders = 256;            // warps 0-7
@@ -71,7 +73,7 @@ struct TcTilt {
   float pad;
 };
 
-constexpr size_t kSmemBytes = 1024 + (size_t)kSB * kStageBytes + (size_t)kTcMaxTilts * sizeof(TcTilt);
+constexpr size_t kSmemBytes = 1024 + (size_t)kSB * kSlabBytes + (size_t)kTcMaxTilts * sizeof(TcTilt);
 
 __device__ __forceinline__ unsigned sa(const void *p) {
   return (unsigned)__cvta_generic_to_shared(p);
@@ -188,7 +190,7 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
   const unsigned limit = a.wait_limit ? a.wait_limit : kBpWaitLimit;
   // 1024-aligned windows (the 64-byte swizzle repeats every 512 bytes), then the tilt table
   unsigned char *win = smem_raw + ((1024u - (sa(smem_raw) & 1023u)) & 1023u);
-  TcTilt *tab = (TcTilt *)(win + (size_t)kSB * kStageBytes);
+  TcTilt *tab = (TcTilt *)(win + (size_t)kSB * kSlabBytes);
 
   const int ntx = (a.X + kTX - 1) / kTX;
   const int x0 = (blockIdx.x % ntx) * kTX, z0 = (blockIdx.x / ntx) * kTZ;
@@ -262,18 +264,29 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
   if (warp == 8) {
     // ---- TMA producer
     if (lane == 0) {
+      const int yrow = a.y_begin + y0;
+      auto prefetch = [&](int i) {
+        const TcTilt tp = tab[i];
+        for (int s = 0; s < tp.nk; ++s)
+          asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(
+                           &map),
+                       "r"(tp.u0), "r"(yrow), "r"((tp.k0 + s) * a.T + i)
+                       : "memory");
+      };
+      for (int i = 0; i < min(kPrefetch, a.T); ++i) prefetch(i);
+      int n = 0;  // windows issued so far: slot n % kSB, its use n / kSB
       for (int i = 0; i < a.T; ++i) {
-        const int b = i % kSB;
-        bar_wait(&empty_b[b], ((i / kSB) & 1) ^ 1, limit, a.err);
+        if (i + kPrefetch < a.T) prefetch(i + kPrefetch);
         const TcTilt tt = tab[i];
-        bar_expect_tx(&full_b[b], (unsigned)(tt.nk * kSlabBytes));
-        for (int s = 0; s < tt.nk; ++s) {
-          const unsigned dst = sa(win + (size_t)b * kStageBytes + (size_t)s * kSlabBytes);
-          const int plane = (tt.k0 + s) * a.T + i;
+        for (int s = 0; s < tt.nk; ++s, ++n) {
+          const int b = n % kSB;
+          bar_wait(&empty_b[b], ((n / kSB) & 1) ^ 1, limit, a.err);
+          bar_expect_tx(&full_b[b], (unsigned)kSlabBytes);
           asm volatile(
               "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes "
-              "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
-              "l"(&map), "r"(tt.u0), "r"(a.y_begin + y0), "r"(plane), "r"(sa(&full_b[b]))
+              "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(sa(win + (size_t)b * kSlabBytes)),
+              "l"(&map), "r"(tt.u0), "r"(yrow), "r"((tt.k0 + s) * a.T + i),
+              "r"(sa(&full_b[b]))
               : "memory");
         }
       }
@@ -281,19 +294,22 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
   } else if (warp == 9) {
     // ---- MMA issuer
     if (lane == 0) {
+      int n = 0;  // windows consumed so far (the producer's order)
       for (int i = 0; i < a.T; ++i) {
-        const int b = i % kSB, s_a = i % kSA;
+        const int s_a = i % kSA;
         bar_wait(&full_a[s_a], (i / kSA) & 1, limit, a.err);
-        bar_wait(&full_b[b], (i / kSB) & 1, limit, a.err);
-        tc_fence_after();
         const int nk = tab[i].nk;
-        const unsigned wbase = sa(win + (size_t)b * kStageBytes);
-        for (int s = 0; s < nk; ++s)
+        for (int s = 0; s < nk; ++s, ++n) {
+          const int b = n % kSB;
+          bar_wait(&full_b[b], (n / kSB) & 1, limit, a.err);
+          tc_fence_after();
+          const unsigned wbase = sa(win + (size_t)b * kSlabBytes);
           for (int kk = 0; kk < 2; ++kk)
             mma(tmem, tmem + kNR + s_a * kACols + s * (kKW / 2) + kk * 8,
-                b_desc(wbase + s * kSlabBytes + kk * 32), (i | s | kk) != 0 ? 1u : 0u);
+                b_desc(wbase + kk * 32), (i | s | kk) != 0 ? 1u : 0u);
+          mma_commit(&empty_b[b]);  // the slot is free once these MMAs complete
+        }
         mma_commit(&empty_a[s_a]);
-        mma_commit(&empty_b[b]);
       }
       mma_commit(&done_bar);
     }
