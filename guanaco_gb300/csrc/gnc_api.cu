@@ -422,10 +422,11 @@ std::string plan_key(const gnc_fbp_desc *d) {
   a.dscale = dscale;
   a.uniform_centre = uniform ? 1 : 0;
   char buf[256];
-  snprintf(buf, sizeof buf, "%zu,%zu,%zu,%zu,%zu,%zu,%d,%d,%d,%d", d->num_angles, d->height,
+  snprintf(buf, sizeof buf, "%zu,%zu,%zu,%zu,%zu,%zu,%d,%d,%d,%d,%d", d->num_angles, d->height,
            d->width, d->grid_height, d->grid_width, d->num_defocus, d->input,
            (d->input == GNC_INPUT_RAW && d->correct) ? 1 : 0, a.staging,
-           backproject_fast_variant(a));
+           backproject_fast_variant(a),
+           a.staging == GNC_STAGE_F16T ? tc_rows(dscale, (int)d->num_defocus) : 0);
   return buf;
 }
 
@@ -571,7 +572,8 @@ static int plan_create(const gnc_fbp_desc *d, cudaMemPool_t pool, cudaStream_t a
     if (e == cudaSuccess) e = dalloc(p, (__half **)&p->staged, elems);
     if (e == cudaSuccess) e = dalloc(p, &p->tilt_exp, (size_t)p->T);
     if (e == cudaSuccess) e = dalloc(p, &p->tilt_part, (size_t)p->T * kTiltPartsMax);
-    if (e == cudaSuccess) e = make_tc_map(p->staged, p->D, p->T, p->H, p->W, &p->tc_map);
+    if (e == cudaSuccess)
+      e = make_tc_map(p->staged, p->D, p->T, p->H, p->W, tc_rows(p->dscale, p->D), &p->tc_map);
   } else {
     // +8 pixels: a 16-byte aligned bulk copy of the last row may run past its end
     const size_t elems = (size_t)p->Y2 * p->D * p->T * p->W + 8;
@@ -728,7 +730,7 @@ int gnc_fbp_backproject_staged(gnc_fbp_plan *p, const void *d_staged, const int8
     a.row_exp = nullptr;
     a.tilt_exp = d_row_exp;
     TcMap map;
-    GNC_CUDA(make_tc_map(d_staged, p->D, p->T, p->H, p->W, &map));
+    GNC_CUDA(make_tc_map(d_staged, p->D, p->T, p->H, p->W, p->tc_map.rows, &map));
     GNC_CUDA(backproject(p, a, exact != 0, s, &map));
     return GNC_OK;
   }

@@ -47,18 +47,28 @@ namespace gnc {
 
 namespace {
 
-constexpr int kTX = 16, kTZ = 8;          // voxel tile (x, z): 128 voxels = M
-constexpr int kNR = 256;                  // Y rows per block = N
-constexpr int kKW = 32;                   // window pixels (two K = 16 steps)
-constexpr int kKMAX = 3;                  // slabs per tile and tilt
-constexpr int kSB = 8, kSA = 4;           // window slots (one slab each), weight stages
-constexpr int kPrefetch = 8;              // tilts whose windows are prefetched into L2 ahead
-constexpr int kSlabBytes = kNR * kKW * 2;  // 16 KB: one slab's window
-constexpr int kACols = kKMAX * (kKW / 2);  // tensor-memory columns of one weight stage
-constexpr int kTmemCols = 512;            // 256 accumulator + 4 x 48 weight columns
-constexpr int kBuilders = 256;            // warps 0-7
+constexpr int kTX = 16, kTZ = 8;  // voxel tile (x, z): 128 voxels = M
+constexpr int kKW = 32;           // window pixels (two K = 16 steps)
+constexpr int kG = 2;             // tilts per group: one barrier round trip per group
+constexpr int kS = 3;             // group stages (windows in shared memory, weights in tensor memory)
+constexpr int kPrefetch = 8;      // tilts whose windows are prefetched into L2 ahead
+constexpr int kBuilders = 256;    // warps 0-7
 constexpr int kThreads = kBuilders + 64;  // + TMA warp + MMA warp
+constexpr int kTmemCols = 512;
 constexpr unsigned kHintNs = 1000;
+
+// The two shapes: 256 rows with at most 2 slabs per tile and tilt, or (for
+// thinner slabs) 128 rows with at most 3.
+template <int NR, int KMAX>
+struct TcShape {
+  static constexpr int kSlabBytes = NR * kKW * 2;                // one slab's window
+  static constexpr int kStageBytes = kG * KMAX * kSlabBytes;     // one group's windows
+  static constexpr int kACols = kG * KMAX * (kKW / 2);           // one group's weights
+  static_assert(NR + kS * kACols <= kTmemCols, "tensor memory");
+  static constexpr size_t kSmem = 1024 + (size_t)kS * kStageBytes + (size_t)kTcMaxTilts * 32;
+  static_assert(kSmem <= 227 * 1024, "shared memory");
+  static constexpr unsigned kIdesc = (1u << 4) | ((unsigned)(NR >> 3) << 17) | ((128u >> 4) << 24);
+};
 
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
 constexpr int kMagicBits = 0x4B400000;
@@ -73,7 +83,6 @@ struct TcTilt {
   float pad;
 };
 
-constexpr size_t kSmemBytes = 1024 + (size_t)kSB * kSlabBytes + (size_t)kTcMaxTilts * sizeof(TcTilt);
 
 __device__ __forceinline__ unsigned sa(const void *p) {
   return (unsigned)__cvta_generic_to_shared(p);
@@ -132,14 +141,14 @@ __device__ __forceinline__ u64 b_desc(unsigned addr) {
   d |= (u64)4 << 61;            // 64-byte swizzle
   return d;
 }
-// Instruction descriptor: FP16 A and B (K-major), FP32 D, M = 128, N = kNR.
-constexpr unsigned kIdesc = (1u << 4) | ((unsigned)(kNR >> 3) << 17) | ((128u >> 4) << 24);
-
-__device__ __forceinline__ void mma(unsigned d_tmem, unsigned a_tmem, u64 bdesc, unsigned acc) {
+// Instruction descriptor: FP16 A and B (K-major), FP32 D, M = 128, N rows
+// (TcShape::kIdesc).
+__device__ __forceinline__ void mma(unsigned d_tmem, unsigned a_tmem, u64 bdesc, unsigned idesc,
+                                    unsigned acc) {
   asm volatile(
       "{ .reg .pred p; setp.ne.u32 p, %4, 0; "
       "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p; }" ::"r"(d_tmem),
-      "r"(a_tmem), "l"(bdesc), "r"(kIdesc), "r"(acc));
+      "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(acc));
 }
 __device__ __forceinline__ void mma_commit(u64 *b) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -176,25 +185,30 @@ __device__ __forceinline__ void tmem_ld32(unsigned taddr, unsigned (&v)[32]) {
 
 }  // namespace
 
+template <int NR, int KMAX>
 __global__ void __launch_bounds__(kThreads, 1)
 k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
+  using P = TcShape<NR, KMAX>;
   if (a.dyn) {
     a.dscale = a.dyn[0];
     a.doffset = a.dyn[1];
   }
   extern __shared__ unsigned char smem_raw[];
-  __shared__ __align__(8) u64 full_b[kSB], empty_b[kSB], full_a[kSA], empty_a[kSA], done_bar;
+  // full[g]: the 256 builders and the TMA producer arrive (plus the windows'
+  // bytes); empty[g]: the MMAs of the group have completed
+  __shared__ __align__(8) u64 full[kS], empty[kS], done_bar;
   __shared__ unsigned tmem_base;
   __shared__ int s_e0;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const unsigned limit = a.wait_limit ? a.wait_limit : kBpWaitLimit;
   // 1024-aligned windows (the 64-byte swizzle repeats every 512 bytes), then the tilt table
   unsigned char *win = smem_raw + ((1024u - (sa(smem_raw) & 1023u)) & 1023u);
-  TcTilt *tab = (TcTilt *)(win + (size_t)kSB * kSlabBytes);
+  TcTilt *tab = (TcTilt *)(win + (size_t)kS * P::kStageBytes);
 
   const int ntx = (a.X + kTX - 1) / kTX;
   const int x0 = (blockIdx.x % ntx) * kTX, z0 = (blockIdx.x / ntx) * kTZ;
-  const int y0 = blockIdx.y * kNR;
+  const int y0 = blockIdx.y * NR;
+  const int ngroups = (a.T + kG - 1) / kG;
 
   if (warp == 9) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -203,13 +217,9 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    for (int i = 0; i < kSB; ++i) {
-      bar_init(&full_b[i], 1);
-      bar_init(&empty_b[i], 1);
-    }
-    for (int i = 0; i < kSA; ++i) {
-      bar_init(&full_a[i], kBuilders);
-      bar_init(&empty_a[i], 1);
+    for (int i = 0; i < kS; ++i) {
+      bar_init(&full[i], kBuilders + 1);
+      bar_init(&empty[i], 1);
     }
     bar_init(&done_bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -241,8 +251,8 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
     tt.u0 = p_lo & ~7;  // round down to a multiple of 8 (also for negative p_lo)
     tt.k0 = k_lo;
     tt.nk = k_hi - k_lo + 1;
-    if (tt.nk > kKMAX) {  // excluded by backproject_tc_supported
-      tt.nk = kKMAX;
+    if (tt.nk > KMAX) {  // excluded by the host's choice of shape
+      tt.nk = KMAX;
       if (a.err) atomicOr(a.err, 2);
     }
     tt.wfac = 0.f;
@@ -262,7 +272,7 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
   const unsigned tmem = tmem_base;
 
   if (warp == 8) {
-    // ---- TMA producer
+    // ---- TMA producer: group g's windows into stage g % kS
     if (lane == 0) {
       const int yrow = a.y_begin + y0;
       auto prefetch = [&](int i) {
@@ -274,42 +284,46 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
                        : "memory");
       };
       for (int i = 0; i < min(kPrefetch, a.T); ++i) prefetch(i);
-      int n = 0;  // windows issued so far: slot n % kSB, its use n / kSB
-      for (int i = 0; i < a.T; ++i) {
-        if (i + kPrefetch < a.T) prefetch(i + kPrefetch);
-        const TcTilt tt = tab[i];
-        for (int s = 0; s < tt.nk; ++s, ++n) {
-          const int b = n % kSB;
-          bar_wait(&empty_b[b], ((n / kSB) & 1) ^ 1, limit, a.err);
-          bar_expect_tx(&full_b[b], (unsigned)kSlabBytes);
-          asm volatile(
-              "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes "
-              "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(sa(win + (size_t)b * kSlabBytes)),
-              "l"(&map), "r"(tt.u0), "r"(yrow), "r"((tt.k0 + s) * a.T + i),
-              "r"(sa(&full_b[b]))
-              : "memory");
+      for (int g = 0; g < ngroups; ++g) {
+        const int st = g % kS;
+        bar_wait(&empty[st], ((g / kS) & 1) ^ 1, limit, a.err);
+        unsigned bytes = 0;
+        for (int j = 0; j < kG && g * kG + j < a.T; ++j) bytes += tab[g * kG + j].nk * P::kSlabBytes;
+        bar_expect_tx(&full[st], bytes);  // the producer's arrival, with the bytes to come
+        for (int j = 0; j < kG && g * kG + j < a.T; ++j) {
+          const int i = g * kG + j;
+          if (i + kPrefetch < a.T) prefetch(i + kPrefetch);
+          const TcTilt tt = tab[i];
+          for (int s = 0; s < tt.nk; ++s) {
+            const unsigned dst =
+                sa(win + (size_t)st * P::kStageBytes + (size_t)(j * KMAX + s) * P::kSlabBytes);
+            asm volatile(
+                "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes "
+                "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+                "l"(&map), "r"(tt.u0), "r"(yrow), "r"((tt.k0 + s) * a.T + i), "r"(sa(&full[st]))
+                : "memory");
+          }
         }
       }
     }
   } else if (warp == 9) {
-    // ---- MMA issuer
+    // ---- MMA issuer: one wait and one commit per group
     if (lane == 0) {
-      int n = 0;  // windows consumed so far (the producer's order)
-      for (int i = 0; i < a.T; ++i) {
-        const int s_a = i % kSA;
-        bar_wait(&full_a[s_a], (i / kSA) & 1, limit, a.err);
-        const int nk = tab[i].nk;
-        for (int s = 0; s < nk; ++s, ++n) {
-          const int b = n % kSB;
-          bar_wait(&full_b[b], (n / kSB) & 1, limit, a.err);
-          tc_fence_after();
-          const unsigned wbase = sa(win + (size_t)b * kSlabBytes);
-          for (int kk = 0; kk < 2; ++kk)
-            mma(tmem, tmem + kNR + s_a * kACols + s * (kKW / 2) + kk * 8,
-                b_desc(wbase + kk * 32), (i | s | kk) != 0 ? 1u : 0u);
-          mma_commit(&empty_b[b]);  // the slot is free once these MMAs complete
+      for (int g = 0; g < ngroups; ++g) {
+        const int st = g % kS;
+        bar_wait(&full[st], (g / kS) & 1, limit, a.err);
+        tc_fence_after();
+        const unsigned wbase = sa(win + (size_t)st * P::kStageBytes);
+        const unsigned abase = tmem + NR + st * P::kACols;
+        for (int j = 0; j < kG && g * kG + j < a.T; ++j) {
+          const int nk = tab[g * kG + j].nk;
+          for (int s = 0; s < nk; ++s)
+            for (int kk = 0; kk < 2; ++kk)
+              mma(tmem, abase + (j * KMAX + s) * (kKW / 2) + kk * 8,
+                  b_desc(wbase + (j * KMAX + s) * P::kSlabBytes + kk * 32), P::kIdesc,
+                  (g | j | s | kk) != 0 ? 1u : 0u);
         }
-        mma_commit(&empty_a[s_a]);
+        mma_commit(&empty[st]);  // the stage is free once these MMAs complete
       }
       mma_commit(&done_bar);
     }
@@ -322,51 +336,67 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
     const bool inside = x < a.X && z < a.Z;
     const float xf = voxel_coordf(x, a.X), zf = voxel_coordf(z, a.Z);
     const unsigned lane_addr = (unsigned)(32 * (warp & 3)) << 16;
-    for (int i = 0; i < a.T; ++i) {
-      const int s_a = i % kSA;
-      const TcTilt tt = tab[i];
-      const float q = detector_coord(__fmul_rn(xf, tt.cos_a), __fmul_rn(zf, tt.sin_a), tt.off);
-      const float r = __fadd_rd(q, kMagic);
-      const int fl = __float_as_int(r) - kMagicBits;
-      const float tw = __fsub_rn(q, __fsub_rn(r, kMagic));
-      const int k = tt.nk > 1 ? slab_index(xf, zf, tt.sin_a, tt.cos_a, a.dscale, a.doffset, a.D)
-                              : tt.k0;
-      const int pos = fl - tt.u0;
-      // the reference skips samples unless 0 <= floor <= N - 2
-      bool valid = inside && fl >= 0 && fl <= a.N - 2;
-      if (valid && (pos < 0 || pos > kKW - 2)) {  // excluded by the tile's window
-        valid = false;
-        if (a.err) atomicOr(a.err, 4);
+    for (int g = 0; g < ngroups; ++g) {
+      const int st = g % kS;
+      // the group's weights first (independent tilts: their arithmetic
+      // interleaves), then the wait for the stage
+      unsigned lo[kG], hi[kG];
+      int idx[kG], blk[kG];
+#pragma unroll
+      for (int j = 0; j < kG; ++j) {
+        const int i = min(g * kG + j, a.T - 1);
+        const TcTilt tt = tab[i];
+        const float q = detector_coord(__fmul_rn(xf, tt.cos_a), __fmul_rn(zf, tt.sin_a), tt.off);
+        const float r = __fadd_rd(q, kMagic);
+        const int fl = __float_as_int(r) - kMagicBits;
+        const float tw = __fsub_rn(q, __fsub_rn(r, kMagic));
+        const int k = tt.nk > 1 ? slab_index(xf, zf, tt.sin_a, tt.cos_a, a.dscale, a.doffset, a.D)
+                                : tt.k0;
+        const int pos = fl - tt.u0;
+        // the reference skips samples unless 0 <= floor <= N - 2
+        bool valid = inside && fl >= 0 && fl <= a.N - 2;
+        if (valid && (pos < 0 || pos > kKW - 2)) {  // excluded by the tile's window
+          valid = false;
+          if (a.err) atomicOr(a.err, 4);
+        }
+        const unsigned h0 =
+            __half_as_ushort(__float2half_rn(__fmul_rn(__fsub_rn(1.f, tw), tt.wfac)));
+        const unsigned h1 = __half_as_ushort(__float2half_rn(__fmul_rn(tw, tt.wfac)));
+        const u64 pair = (u64)(h0 | (h1 << 16)) << ((pos & 1) * 16);
+        lo[j] = (unsigned)pair;
+        hi[j] = (unsigned)(pair >> 32);
+        idx[j] = (pos >> 1) - 8 * h;            // word of this half holding the pixel pair
+        blk[j] = valid ? k - tt.k0 : -1;        // the slab block holding the weights
       }
-      const unsigned h0 = __half_as_ushort(__float2half_rn(__fmul_rn(__fsub_rn(1.f, tw), tt.wfac)));
-      const unsigned h1 = __half_as_ushort(__float2half_rn(__fmul_rn(tw, tt.wfac)));
-      const u64 pair = (u64)(h0 | (h1 << 16)) << ((pos & 1) * 16);
-      const unsigned lo = (unsigned)pair, hi = (unsigned)(pair >> 32);
-      const int idx = (pos >> 1) - 8 * h;  // word of this half holding the pixel pair
-      // the weights first, then the wait for the buffer: the arithmetic above
-      // overlaps the MMAs still reading it
-      bar_wait(&empty_a[s_a], ((i / kSA) & 1) ^ 1, limit, a.err);
+      bar_wait(&empty[st], ((g / kS) & 1) ^ 1, limit, a.err);
       tc_fence_after();
+      const unsigned abase = tmem + lane_addr + NR + st * P::kACols + 8 * h;
 #pragma unroll
-      for (int s = 0; s < kKMAX; ++s) {
-        if (s < tt.nk) {
-          const bool mine = valid && (k - tt.k0 == s);
-          unsigned w[8];
+      for (int j = 0; j < kG; ++j) {
+        if (g * kG + j >= a.T) break;
+        const int nk = tab[g * kG + j].nk;
 #pragma unroll
-          for (int j = 0; j < 8; ++j) w[j] = !mine ? 0u : (j == idx ? lo : (j == idx + 1 ? hi : 0u));
-          tmem_st8(tmem + lane_addr + kNR + s_a * kACols + s * (kKW / 2) + 8 * h, w);
+        for (int s = 0; s < KMAX; ++s) {
+          if (s < nk) {
+            const bool mine = blk[j] == s;
+            unsigned w[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+              w[q] = !mine ? 0u : (q == idx[j] ? lo[j] : (q == idx[j] + 1 ? hi[j] : 0u));
+            tmem_st8(abase + (j * KMAX + s) * (kKW / 2), w);
+          }
         }
       }
       asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       tc_fence_before();
-      bar_arrive(&full_a[s_a]);
+      bar_arrive(&full[st]);
     }
     // ---- store: the accumulator of voxel m; this thread's half of the rows
     bar_wait(&done_bar, 0, limit, a.err);
     tc_fence_after();
     const float sc = a.geom[0].scale * pow2f(max(-126, min(127, -e0)));
 #pragma unroll 1
-    for (int c = h * (kNR / 2); c < (h + 1) * (kNR / 2); c += 32) {
+    for (int c = h * (NR / 2); c < (h + 1) * (NR / 2); c += 32) {
       unsigned v[32];
       tmem_ld32(tmem + lane_addr + (unsigned)c, v);
       if (inside) {
@@ -446,23 +476,31 @@ cudaError_t launch_tilt_exponents(const float *input, size_t per_tilt, int t0, i
   return cudaGetLastError();
 }
 
-bool backproject_tc_supported(int N, int T, float dscale, int D, bool uniform_centre) {
-  if (!uniform_centre || N % 8 != 0 || N < 2 || T < 1 || T > kTcMaxTilts) return false;
-  if (D <= 1) return true;
-  // the voxel centres of a 16 x 8 tile span at most sqrt(15^2 + 7^2) pixels in
-  // height (plus one for rounding); slabs are 1 / dscale pixels thick
+// Slabs a 16 x 8 tile can reach for one tilt: the voxel centres span at most
+// sqrt(15^2 + 7^2) pixels in height (plus one for rounding); slabs are
+// 1 / dscale pixels thick.
+static int tc_slabs_per_tile(float dscale, int D) {
+  if (D <= 1) return 1;
   const double span =
       std::sqrt((double)(kTX - 1) * (kTX - 1) + (double)(kTZ - 1) * (kTZ - 1)) + 1.0;
-  return (int)std::ceil(span * std::fabs((double)dscale)) + 1 <= kKMAX;
+  return (int)std::ceil(span * std::fabs((double)dscale)) + 1;
 }
+
+bool backproject_tc_supported(int N, int T, float dscale, int D, bool uniform_centre) {
+  if (!uniform_centre || N % 8 != 0 || N < 2 || T < 1 || T > kTcMaxTilts) return false;
+  return tc_slabs_per_tile(dscale, D) <= 3;
+}
+
+// Rows per block of the shape a geometry uses: 256 (up to 2 slabs per tile), else 128.
+int tc_rows(float dscale, int D) { return tc_slabs_per_tile(dscale, D) <= 2 ? 256 : 128; }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
                                   const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-cudaError_t make_tc_map(const void *staged, int D, int T, int H, int N, TcMap *out) {
-  static_assert(sizeof(CUtensorMap) == sizeof(TcMap), "tensor map size");
+cudaError_t make_tc_map(const void *staged, int D, int T, int H, int N, int rows, TcMap *out) {
+  static_assert(sizeof(CUtensorMap) == sizeof(TcMap::bytes), "tensor map size");
   static EncodeTiledFn encode = nullptr;
   if (!encode) {
     void *fn = nullptr;
@@ -473,10 +511,10 @@ cudaError_t make_tc_map(const void *staged, int D, int T, int H, int N, TcMap *o
     if (!fn || q != cudaDriverEntryPointSuccess) return cudaErrorNotSupported;
     encode = (EncodeTiledFn)fn;
   }
-  // rows (D T, H, N) of FP16; box: 32 pixels x kNR rows x 1 (64-byte rows, swizzled)
+  // rows (D T, H, N) of FP16; box: 32 pixels x `rows` rows x 1 (64-byte rows, swizzled)
   cuuint64_t dims[3] = {(cuuint64_t)N, (cuuint64_t)H, (cuuint64_t)D * T};
   cuuint64_t strides[2] = {(cuuint64_t)N * 2, (cuuint64_t)H * N * 2};
-  cuuint32_t box[3] = {(cuuint32_t)kKW, (cuuint32_t)kNR, 1};
+  cuuint32_t box[3] = {(cuuint32_t)kKW, (cuuint32_t)rows, 1};
   cuuint32_t es[3] = {1, 1, 1};
   CUtensorMap m;
   std::memset(&m, 0, sizeof m);
@@ -486,17 +524,26 @@ cudaError_t make_tc_map(const void *staged, int D, int T, int H, int N, TcMap *o
                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
   std::memcpy(out->bytes, &m, sizeof m);
+  out->rows = rows;
   return cudaSuccess;
 }
 
-cudaError_t launch_backproject_tc(const BpArgs &a, const TcMap &map, cudaStream_t s) {
-  if (cudaError_t e = ensure_dynamic_smem<k_bp_tc>((int)kSmemBytes)) return e;
+template <int NR, int KMAX>
+static cudaError_t launch_tc(const BpArgs &a, const TcMap &map, cudaStream_t s) {
+  using P = TcShape<NR, KMAX>;
+  if (cudaError_t e = ensure_dynamic_smem<k_bp_tc<NR, KMAX>>((int)P::kSmem)) return e;
   const int ntx = (a.X + kTX - 1) / kTX, ntz = (a.Z + kTZ - 1) / kTZ;
-  dim3 grid(ntx * ntz, (a.Y + kNR - 1) / kNR);
+  dim3 grid(ntx * ntz, (a.Y + NR - 1) / NR);
   CUtensorMap m;
   std::memcpy(&m, map.bytes, sizeof m);
-  k_bp_tc<<<grid, kThreads, kSmemBytes, s>>>(a, m);
+  k_bp_tc<NR, KMAX><<<grid, kThreads, P::kSmem, s>>>(a, m);
   return cudaGetLastError();
+}
+
+cudaError_t launch_backproject_tc(const BpArgs &a, const TcMap &map, cudaStream_t s) {
+  // the map's box height is the shape's row count
+  if (map.rows != tc_rows(a.dscale, a.D)) return cudaErrorInvalidValue;
+  return map.rows == 256 ? launch_tc<256, 2>(a, map, s) : launch_tc<128, 3>(a, map, s);
 }
 
 }  // namespace gnc

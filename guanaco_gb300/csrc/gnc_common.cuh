@@ -225,8 +225,12 @@ bool backproject_tc_supported(int N, int T, float dscale, int D, bool uniform_ce
 // passed to the kernel by value.
 struct TcMap {
   alignas(64) unsigned char bytes[128];
+  int rows;  // Y rows of one tile (the kernel shape it serves)
 };
-cudaError_t make_tc_map(const void *staged, int D, int T, int H, int N, TcMap *out);
+// Rows per block of the kernel shape for this slab map: 256 (at most two slabs
+// per tile and tilt) or 128 (three).
+int tc_rows(float dscale, int D);
+cudaError_t make_tc_map(const void *staged, int D, int T, int H, int N, int rows, TcMap *out);
 cudaError_t launch_backproject_tc(const BpArgs &a, const TcMap &map, cudaStream_t s);
 // Per-tilt F16T exponents of the input (T tilts of `per_tilt` floats, tilts
 // [t0, t0 + nt)): exp[t] = f16t_exponent(||input_t||^2, factor[t], gain);
