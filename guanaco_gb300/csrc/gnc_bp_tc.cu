@@ -29,13 +29,16 @@
 // Warp roles (320 threads, one block per SM): warps 0-7 build weights
 // (warps w and w + 4 the two window halves of voxels 32 (w % 4) ..) and store
 // the volume, warp 8 issues the TMA loads, warp 9 owns the tensor memory and
-// issues the MMAs.  A ring of kSB shared-memory window slots (a tilt takes
-// one per slab it reaches, mostly one) and kSA tensor-memory weight stages,
-// each with a "full" and an "empty" mbarrier; the windows of the tilt
-// kPrefetch ahead are prefetched into L2, so the loads find them there.  The
-// builders compute a tilt's weights before they wait for its buffer, and read
-// the tilt's geometry from a shared-memory table filled once per block.  Every
-// wait is bounded and records a timeout in the plan's error word.
+// issues the MMAs.  Tilts go in groups of kG; each of kS group stages holds a
+// group's windows in shared memory and its weights in tensor memory, with one
+// "full" mbarrier (the builders and the producer arrive, the windows' bytes
+// complete it) and one "empty" mbarrier (the MMAs' commit), so a group costs
+// one barrier round trip and one commit.  The builders compute a group's
+// weights before they wait for its stage, and read the tilts' geometry from a
+// shared-memory table filled once per block.  (Prefetching the windows of
+// later tilts into L2 was measured and made the kernel 25 % slower: the
+// prefetches compete with the loads.)  Every wait is bounded and records a
+// timeout in the plan's error word.
 #include <cuda.h>
 
 #include <cmath>
@@ -51,9 +54,11 @@ constexpr int kTX = 16, kTZ = 8;  // voxel tile (x, z): 128 voxels = M
 constexpr int kKW = 32;           // window pixels (two K = 16 steps)
 constexpr int kG = 2;             // tilts per group: one barrier round trip per group
 constexpr int kS = 3;             // group stages (windows in shared memory, weights in tensor memory)
-constexpr int kPrefetch = 8;      // tilts whose windows are prefetched into L2 ahead
-constexpr int kBuilders = 256;    // warps 0-7
+constexpr int kQ = 2;             // builder threads per voxel (parts of the window)
+constexpr int kWords = kKW / 2 / kQ;  // tensor-memory columns one builder thread writes
+constexpr int kBuilders = 128 * kQ;       // warps 0 .. 4 kQ - 1
 constexpr int kThreads = kBuilders + 64;  // + TMA warp + MMA warp
+constexpr int kWarpTma = kBuilders / 32, kWarpMma = kWarpTma + 1;
 constexpr int kTmemCols = 512;
 constexpr unsigned kHintNs = 1000;
 
@@ -170,6 +175,12 @@ __device__ __forceinline__ void tmem_st8(unsigned taddr, const unsigned (&r)[8])
       "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])
       : "memory");
 }
+__device__ __forceinline__ void tmem_st(unsigned taddr, const unsigned (&r)[8]) { tmem_st8(taddr, r); }
+__device__ __forceinline__ void tmem_st(unsigned taddr, const unsigned (&r)[4]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(taddr),
+               "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3])
+               : "memory");
+}
 __device__ __forceinline__ void tmem_ld32(unsigned taddr, unsigned (&v)[32]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
@@ -210,7 +221,7 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
   const int y0 = blockIdx.y * NR;
   const int ngroups = (a.T + kG - 1) / kG;
 
-  if (warp == 9) {
+  if (warp == kWarpMma) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      sa(&tmem_base)),
                  "r"((unsigned)kTmemCols));
@@ -271,19 +282,10 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
   __syncthreads();
   const unsigned tmem = tmem_base;
 
-  if (warp == 8) {
+  if (warp == kWarpTma) {
     // ---- TMA producer: group g's windows into stage g % kS
     if (lane == 0) {
       const int yrow = a.y_begin + y0;
-      auto prefetch = [&](int i) {
-        const TcTilt tp = tab[i];
-        for (int s = 0; s < tp.nk; ++s)
-          asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(
-                           &map),
-                       "r"(tp.u0), "r"(yrow), "r"((tp.k0 + s) * a.T + i)
-                       : "memory");
-      };
-      for (int i = 0; i < min(kPrefetch, a.T); ++i) prefetch(i);
       for (int g = 0; g < ngroups; ++g) {
         const int st = g % kS;
         bar_wait(&empty[st], ((g / kS) & 1) ^ 1, limit, a.err);
@@ -292,7 +294,6 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
         bar_expect_tx(&full[st], bytes);  // the producer's arrival, with the bytes to come
         for (int j = 0; j < kG && g * kG + j < a.T; ++j) {
           const int i = g * kG + j;
-          if (i + kPrefetch < a.T) prefetch(i + kPrefetch);
           const TcTilt tt = tab[i];
           for (int s = 0; s < tt.nk; ++s) {
             const unsigned dst =
@@ -306,7 +307,7 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
         }
       }
     }
-  } else if (warp == 9) {
+  } else if (warp == kWarpMma) {
     // ---- MMA issuer: one wait and one commit per group
     if (lane == 0) {
       for (int g = 0; g < ngroups; ++g) {
@@ -329,8 +330,8 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
     }
   } else {
     // ---- weight builders: voxel m = (x0 + m % 16, z0 + m / 16) = tensor-memory
-    // lane m; this thread writes the window half h (pixels 16 h .. 16 h + 15,
-    // columns 8 h .. 8 h + 7 of each slab's block)
+    // lane m; this thread writes part h of the window (pixels kKW / kQ h ..,
+    // columns kKW / 2 / kQ h .. of each slab's block)
     const int m = 32 * (warp & 3) + lane, h = warp >> 2;
     const int x = x0 + (m & (kTX - 1)), z = z0 + (m >> 4);
     const bool inside = x < a.X && z < a.Z;
@@ -365,12 +366,12 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
         const u64 pair = (u64)(h0 | (h1 << 16)) << ((pos & 1) * 16);
         lo[j] = (unsigned)pair;
         hi[j] = (unsigned)(pair >> 32);
-        idx[j] = (pos >> 1) - 8 * h;            // word of this half holding the pixel pair
+        idx[j] = (pos >> 1) - kWords * h;       // word of this part holding the pixel pair
         blk[j] = valid ? k - tt.k0 : -1;        // the slab block holding the weights
       }
       bar_wait(&empty[st], ((g / kS) & 1) ^ 1, limit, a.err);
       tc_fence_after();
-      const unsigned abase = tmem + lane_addr + NR + st * P::kACols + 8 * h;
+      const unsigned abase = tmem + lane_addr + NR + st * P::kACols + kWords * h;
 #pragma unroll
       for (int j = 0; j < kG; ++j) {
         if (g * kG + j >= a.T) break;
@@ -379,11 +380,11 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
         for (int s = 0; s < KMAX; ++s) {
           if (s < nk) {
             const bool mine = blk[j] == s;
-            unsigned w[8];
+            unsigned w[kWords];
 #pragma unroll
-            for (int q = 0; q < 8; ++q)
+            for (int q = 0; q < kWords; ++q)
               w[q] = !mine ? 0u : (q == idx[j] ? lo[j] : (q == idx[j] + 1 ? hi[j] : 0u));
-            tmem_st8(abase + (j * KMAX + s) * (kKW / 2), w);
+            tmem_st(abase + (j * KMAX + s) * (kKW / 2), w);
           }
         }
       }
@@ -396,7 +397,7 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
     tc_fence_after();
     const float sc = a.geom[0].scale * pow2f(max(-126, min(127, -e0)));
 #pragma unroll 1
-    for (int c = h * (NR / 2); c < (h + 1) * (NR / 2); c += 32) {
+    for (int c = h * (NR / kQ); c < (h + 1) * (NR / kQ); c += 32) {
       unsigned v[32];
       tmem_ld32(tmem + lane_addr + (unsigned)c, v);
       if (inside) {
@@ -410,7 +411,7 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 9)
+  if (warp == kWarpMma)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"((unsigned)kTmemCols));
 }
