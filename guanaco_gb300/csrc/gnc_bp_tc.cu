@@ -53,25 +53,25 @@ namespace {
 constexpr int kTX = 16, kTZ = 8;  // voxel tile (x, z): 128 voxels = M
 constexpr int kKW = 32;           // window pixels (two K = 16 steps)
 constexpr int kG = 2;             // tilts per group: one barrier round trip per group
-constexpr int kS = 3;             // group stages (windows in shared memory, weights in tensor memory)
 constexpr int kQ = 2;             // builder threads per voxel (parts of the window)
 constexpr int kWords = kKW / 2 / kQ;  // tensor-memory columns one builder thread writes
 constexpr int kBuilders = 128 * kQ;       // warps 0 .. 4 kQ - 1
 constexpr int kThreads = kBuilders + 64;  // + TMA warp + MMA warp
 constexpr int kWarpTma = kBuilders / 32, kWarpMma = kWarpTma + 1;
-constexpr int kTmemCols = 512;
 constexpr unsigned kHintNs = 1000;
 
-// The two shapes: 256 rows with at most 2 slabs per tile and tilt, or (for
-// thinner slabs) 128 rows with at most 3.
-template <int NR, int KMAX>
+// A shape: NR rows, at most KMAX slabs per tile and tilt, S group stages,
+// TMEM tensor-memory columns and BLOCKS blocks per SM.
+template <int NR, int KMAX, int S, int TMEM, int BLOCKS>
 struct TcShape {
+  static constexpr int kS = S, kTmemCols = TMEM;
   static constexpr int kSlabBytes = NR * kKW * 2;                // one slab's window
   static constexpr int kStageBytes = kG * KMAX * kSlabBytes;     // one group's windows
   static constexpr int kACols = kG * KMAX * (kKW / 2);           // one group's weights
   static_assert(NR + kS * kACols <= kTmemCols, "tensor memory");
   static constexpr size_t kSmem = 1024 + (size_t)kS * kStageBytes + (size_t)kTcMaxTilts * 32;
-  static_assert(kSmem <= 227 * 1024, "shared memory");
+  static_assert(kSmem * BLOCKS <= 227 * 1024, "shared memory");
+  static_assert(TMEM * BLOCKS <= 512, "tensor memory per SM");
   static constexpr unsigned kIdesc = (1u << 4) | ((unsigned)(NR >> 3) << 17) | ((128u >> 4) << 24);
 };
 
@@ -196,10 +196,11 @@ __device__ __forceinline__ void tmem_ld32(unsigned taddr, unsigned (&v)[32]) {
 
 }  // namespace
 
-template <int NR, int KMAX>
-__global__ void __launch_bounds__(kThreads, 1)
+template <int NR, int KMAX, int S, int TMEM, int BLOCKS>
+__global__ void __launch_bounds__(kThreads, BLOCKS)
 k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
-  using P = TcShape<NR, KMAX>;
+  using P = TcShape<NR, KMAX, S, TMEM, BLOCKS>;
+  constexpr int kS = P::kS, kTmemCols = P::kTmemCols;
   if (a.dyn) {
     a.dscale = a.dyn[0];
     a.doffset = a.dyn[1];
@@ -492,8 +493,9 @@ bool backproject_tc_supported(int N, int T, float dscale, int D, bool uniform_ce
   return tc_slabs_per_tile(dscale, D) <= 3;
 }
 
-// Rows per block of the shape a geometry uses: 256 (up to 2 slabs per tile), else 128.
-int tc_rows(float dscale, int D) { return tc_slabs_per_tile(dscale, D) <= 2 ? 256 : 128; }
+// Rows per block of the shape a geometry uses (the TMA box height).
+constexpr int kRowsTwoSlabs = 128;
+int tc_rows(float dscale, int D) { return tc_slabs_per_tile(dscale, D) <= 2 ? kRowsTwoSlabs : 128; }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
@@ -529,22 +531,30 @@ cudaError_t make_tc_map(const void *staged, int D, int T, int H, int N, int rows
   return cudaSuccess;
 }
 
-template <int NR, int KMAX>
+template <int NR, int KMAX, int S, int TMEM, int BLOCKS>
 static cudaError_t launch_tc(const BpArgs &a, const TcMap &map, cudaStream_t s) {
-  using P = TcShape<NR, KMAX>;
-  if (cudaError_t e = ensure_dynamic_smem<k_bp_tc<NR, KMAX>>((int)P::kSmem)) return e;
+  using P = TcShape<NR, KMAX, S, TMEM, BLOCKS>;
+  auto kern = k_bp_tc<NR, KMAX, S, TMEM, BLOCKS>;
+  if (cudaError_t e = ensure_dynamic_smem<k_bp_tc<NR, KMAX, S, TMEM, BLOCKS>>((int)P::kSmem))
+    return e;
   const int ntx = (a.X + kTX - 1) / kTX, ntz = (a.Z + kTZ - 1) / kTZ;
   dim3 grid(ntx * ntz, (a.Y + NR - 1) / NR);
   CUtensorMap m;
   std::memcpy(&m, map.bytes, sizeof m);
-  k_bp_tc<NR, KMAX><<<grid, kThreads, P::kSmem, s>>>(a, m);
+  kern<<<grid, kThreads, P::kSmem, s>>>(a, m);
   return cudaGetLastError();
 }
 
 cudaError_t launch_backproject_tc(const BpArgs &a, const TcMap &map, cudaStream_t s) {
   // the map's box height is the shape's row count
   if (map.rows != tc_rows(a.dscale, a.D)) return cudaErrorInvalidValue;
-  return map.rows == 256 ? launch_tc<256, 2>(a, map, s) : launch_tc<128, 3>(a, map, s);
+  // up to two slabs per tile: 256 rows, one block per SM, or 128 rows, two
+  // blocks per SM (one block's set-up and volume stores overlap the other's
+  // tilt loop); three slabs: 128 rows, one block per SM
+  if (tc_slabs_per_tile(a.dscale, a.D) <= 2)
+    return map.rows == 256 ? launch_tc<256, 2, 3, 512, 1>(a, map, s)
+                           : launch_tc<128, 2, 2, 256, 2>(a, map, s);
+  return launch_tc<128, 3, 3, 512, 1>(a, map, s);
 }
 
 }  // namespace gnc
