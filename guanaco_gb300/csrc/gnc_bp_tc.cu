@@ -6,20 +6,22 @@
 // (two non-zeros per voxel: (1 - t) at the voxel's pixel floor(p), t at the
 // next one, src/libguanaco/reconstructor.cpp:76-86) and the staged rows.  A
 // block owns 128 voxels -- a 16 (x) by 8 (z) tile, compact so that for any
-// tilt they project onto at most 18 detector pixels -- and 256 Y rows.  Per
-// tilt and per defocus slab the tile reaches:
-//   * one TMA load brings the 32-pixel window [u0, u0 + 32) of the 256 rows
-//     (u0 a multiple of 8) into shared memory, 64-byte swizzled;
-//   * 256 builder threads (two per voxel, one per half of the window) compute
-//     the voxel's detector coordinate, floor, weight and slab with the
-//     reference's float operations, and store its 32 weights (zero outside
-//     its own slab, its own pixel pair and the detector edge rule) into a
-//     tensor-memory row;
-//   * one thread issues two tcgen05.mma (M 128 voxels, N 256 rows, K 16
-//     pixels each) accumulating into the 128 x 256 FP32 tile in tensor memory.
-// Weights carry the tilt's factor 2^(E0 - e(t)) (E0 the smallest exponent over
-// the tilts), so the accumulator counts in units of 2^-E0 for every tilt; the
-// store multiplies by the backprojection scale and 2^-E0.
+// tilt they project onto at most 18 detector pixels -- and NR Y rows (256
+// when a tile reaches at most two defocus slabs per tilt, 128 for three).
+// Per tilt and per defocus slab the tile reaches, it takes one slot of a ring
+// of R slots in shared memory; a slot holds
+//   * the 32-pixel window [u0, u0 + 32) of the NR rows (u0 a multiple of 8),
+//     brought by one TMA load, 64-byte swizzled (the MMA's B operand);
+//   * the 128 x 32 FP16 weights of the slab (the A operand, K-major, no
+//     swizzle), written by 256 builder threads -- two per voxel, one per half
+//     of the window -- that compute the voxel's detector coordinate, floor,
+//     weight and slab with the reference's float operations, zero their half
+//     row and store the voxel's two weights when its slab is the slot's;
+// and one thread issues two tcgen05.mma per slot (M 128 voxels, N NR rows,
+// K 16 pixels each) accumulating into the 128 x NR FP32 tile in tensor
+// memory.  Weights carry the tilt's factor 2^(E0 - e(t)) (E0 the smallest
+// exponent over the tilts), so the accumulator counts in units of 2^-E0 for
+// every tilt; the store multiplies by the backprojection scale and 2^-E0.
 //
 // What decides which samples a voxel takes -- its detector coordinate, floor,
 // weight t, slab index and edge rule -- is the reference's float arithmetic,
@@ -29,16 +31,20 @@
 // Warp roles (320 threads, one block per SM): warps 0-7 build weights
 // (warps w and w + 4 the two window halves of voxels 32 (w % 4) ..) and store
 // the volume, warp 8 issues the TMA loads, warp 9 owns the tensor memory and
-// issues the MMAs.  Tilts go in groups of kG; each of kS group stages holds a
-// group's windows in shared memory and its weights in tensor memory, with one
-// "full" mbarrier (the builders and the producer arrive, the windows' bytes
-// complete it) and one "empty" mbarrier (the MMAs' commit), so a group costs
-// one barrier round trip and one commit.  The builders compute a group's
-// weights before they wait for its stage, and read the tilts' geometry from a
-// shared-memory table filled once per block.  (Prefetching the windows of
-// later tilts into L2 was measured and made the kernel 25 % slower: the
-// prefetches compete with the loads.)  Every wait is bounded and records a
-// timeout in the plan's error word.
+// issues the MMAs.  Tilts go in groups of kG, each with a "full" mbarrier
+// (the builders and the producer arrive, the windows' bytes complete it) and
+// an "empty" one (the MMAs' commit); a group's slots are consecutive in the
+// ring, so before filling them the producer and the builders wait for the
+// one earlier group that last used the newest of them (a per-group table
+// built once per block from the tilts' slab counts).  The builders compute a
+// group's weights before that wait and read the tilts' geometry from a
+// shared-memory table.  Measured on the 61-tilt 1024 x 1024 x 300 ten-slab
+// series: weights in tensor memory (tcgen05.st of all 32 words per voxel)
+// 2.41 ms, weights in shared memory with two 16-byte zero stores and two
+// 2-byte weight stores per thread and slot 2.17 ms.  (Prefetching the windows
+// of later tilts into L2 made the kernel 25 % slower: the prefetches compete
+// with the loads.)  Every wait is bounded and records a timeout in the plan's
+// error word.
 #include <cuda.h>
 
 #include <cmath>
@@ -53,25 +59,26 @@ namespace {
 constexpr int kTX = 16, kTZ = 8;  // voxel tile (x, z): 128 voxels = M
 constexpr int kKW = 32;           // window pixels (two K = 16 steps)
 constexpr int kG = 2;             // tilts per group: one barrier round trip per group
-constexpr int kQ = 2;             // builder threads per voxel (parts of the window)
-constexpr int kWords = kKW / 2 / kQ;  // tensor-memory columns one builder thread writes
-constexpr int kBuilders = 128 * kQ;       // warps 0 .. 4 kQ - 1
+constexpr int kQ = 2;             // builder threads per voxel (window halves)
+constexpr int kBuilders = 128 * kQ;       // warps 0-7
 constexpr int kThreads = kBuilders + 64;  // + TMA warp + MMA warp
 constexpr int kWarpTma = kBuilders / 32, kWarpMma = kWarpTma + 1;
+constexpr int kSB = 8;            // barrier stages (more than the groups in flight)
 constexpr unsigned kHintNs = 1000;
+constexpr int kABytes = 128 * kKW * 2;  // one slab's weights: 128 voxels x 32 pixels, FP16
+constexpr int kAChunk = 128 * 16;       // 8 pixels of all 128 voxels (one K core-matrix column)
 
-// A shape: NR rows, at most KMAX slabs per tile and tilt, S group stages,
-// TMEM tensor-memory columns and BLOCKS blocks per SM.
-template <int NR, int KMAX, int S, int TMEM, int BLOCKS>
+// A shape: NR rows, at most KMAX slabs per tile and tilt, R slots (a slot holds
+// one slab's window and weights; a tilt takes one per slab it reaches).
+template <int NR, int KMAX, int R>
 struct TcShape {
-  static constexpr int kS = S, kTmemCols = TMEM;
-  static constexpr int kSlabBytes = NR * kKW * 2;                // one slab's window
-  static constexpr int kStageBytes = kG * KMAX * kSlabBytes;     // one group's windows
-  static constexpr int kACols = kG * KMAX * (kKW / 2);           // one group's weights
-  static_assert(NR + kS * kACols <= kTmemCols, "tensor memory");
-  static constexpr size_t kSmem = 1024 + (size_t)kS * kStageBytes + (size_t)kTcMaxTilts * 32;
-  static_assert(kSmem * BLOCKS <= 227 * 1024, "shared memory");
-  static_assert(TMEM * BLOCKS <= 512, "tensor memory per SM");
+  static constexpr int kBBytes = NR * kKW * 2;  // one slab's window: NR rows x 32 pixels
+  static constexpr int kTmemCols = NR;          // the accumulator only
+  static_assert(R >= 2 * kG * KMAX, "a slot ring holds two groups");
+  static_assert(R / 2 + 1 < kSB, "waits reach back fewer groups than barrier stages");
+  static constexpr size_t kSmem = 1024 + (size_t)R * (kBBytes + kABytes) +
+                                  (size_t)kTcMaxTilts * 32 + (size_t)(kTcMaxTilts / kG) * 16;
+  static_assert(kSmem <= 227 * 1024, "shared memory");
   static constexpr unsigned kIdesc = (1u << 4) | ((unsigned)(NR >> 3) << 17) | ((128u >> 4) << 24);
 };
 
@@ -85,7 +92,13 @@ struct TcTilt {
   int k0, nk;  // first slab and slab count of the tile
   float wfac;  // 2^(E0 - e(t))
   float cos_a, sin_a, off;  // the tilt's geometry (reconstructor.cpp:35-47)
-  float pad;
+  int slot;    // running slot count of its first slab (slot slot % R)
+};
+
+struct TcGroup {
+  int c, n;    // first running slot and slot count of the group
+  int w;       // the last earlier group that used one of these slots (-1: none)
+  int pad;
 };
 
 
@@ -136,6 +149,15 @@ __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
+// Shared-memory descriptor of a weight block: K-major, no swizzle, 8 x 16-byte
+// core matrices; 8-voxel groups 128 bytes apart, 8-pixel groups kAChunk apart.
+__device__ __forceinline__ u64 a_desc(unsigned addr) {
+  u64 d = (u64)((addr & 0x3FFFFu) >> 4);
+  d |= (u64)(kAChunk >> 4) << 16;  // leading offset: next 8 pixels
+  d |= (u64)(128 >> 4) << 32;      // stride offset: next 8 voxels
+  d |= (u64)1 << 46;               // descriptor version
+  return d;                        // layout 0: no swizzle
+}
 // Shared-memory operand descriptor: K-major, 64-byte swizzle, rows of 64
 // bytes in 8-row atoms of 512 bytes (stride between atoms 512 B).
 __device__ __forceinline__ u64 b_desc(unsigned addr) {
@@ -148,12 +170,12 @@ __device__ __forceinline__ u64 b_desc(unsigned addr) {
 }
 // Instruction descriptor: FP16 A and B (K-major), FP32 D, M = 128, N rows
 // (TcShape::kIdesc).
-__device__ __forceinline__ void mma(unsigned d_tmem, unsigned a_tmem, u64 bdesc, unsigned idesc,
+__device__ __forceinline__ void mma(unsigned d_tmem, u64 adesc, u64 bdesc, unsigned idesc,
                                     unsigned acc) {
   asm volatile(
       "{ .reg .pred p; setp.ne.u32 p, %4, 0; "
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p; }" ::"r"(d_tmem),
-      "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(acc));
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
 }
 __device__ __forceinline__ void mma_commit(u64 *b) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -161,26 +183,6 @@ __device__ __forceinline__ void mma_commit(u64 *b) {
                : "memory");
 }
 
-__device__ __forceinline__ void tmem_st16(unsigned taddr, const unsigned (&r)[16]) {
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
-      "%14,%15,%16};" ::"r"(taddr),
-      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
-      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
-      : "memory");
-}
-__device__ __forceinline__ void tmem_st8(unsigned taddr, const unsigned (&r)[8]) {
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr),
-      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])
-      : "memory");
-}
-__device__ __forceinline__ void tmem_st(unsigned taddr, const unsigned (&r)[8]) { tmem_st8(taddr, r); }
-__device__ __forceinline__ void tmem_st(unsigned taddr, const unsigned (&r)[4]) {
-  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(taddr),
-               "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3])
-               : "memory");
-}
 __device__ __forceinline__ void tmem_ld32(unsigned taddr, unsigned (&v)[32]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
@@ -196,26 +198,28 @@ __device__ __forceinline__ void tmem_ld32(unsigned taddr, unsigned (&v)[32]) {
 
 }  // namespace
 
-template <int NR, int KMAX, int S, int TMEM, int BLOCKS>
-__global__ void __launch_bounds__(kThreads, BLOCKS)
+template <int NR, int KMAX, int R>
+__global__ void __launch_bounds__(kThreads, 1)
 k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
-  using P = TcShape<NR, KMAX, S, TMEM, BLOCKS>;
-  constexpr int kS = P::kS, kTmemCols = P::kTmemCols;
+  using P = TcShape<NR, KMAX, R>;
   if (a.dyn) {
     a.dscale = a.dyn[0];
     a.doffset = a.dyn[1];
   }
   extern __shared__ unsigned char smem_raw[];
-  // full[g]: the 256 builders and the TMA producer arrive (plus the windows'
-  // bytes); empty[g]: the MMAs of the group have completed
-  __shared__ __align__(8) u64 full[kS], empty[kS], done_bar;
+  // full[g % kSB]: the builders and the TMA producer arrive (plus the windows'
+  // bytes); empty[g % kSB]: the MMAs of group g have completed
+  __shared__ __align__(8) u64 full[kSB], empty[kSB], done_bar;
   __shared__ unsigned tmem_base;
   __shared__ int s_e0;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const unsigned limit = a.wait_limit ? a.wait_limit : kBpWaitLimit;
-  // 1024-aligned windows (the 64-byte swizzle repeats every 512 bytes), then the tilt table
-  unsigned char *win = smem_raw + ((1024u - (sa(smem_raw) & 1023u)) & 1023u);
-  TcTilt *tab = (TcTilt *)(win + (size_t)kS * P::kStageBytes);
+  // 1024-aligned windows (the 64-byte swizzle repeats every 512 bytes), then
+  // the weight blocks, the tilt table and the group table
+  unsigned char *bwin = smem_raw + ((1024u - (sa(smem_raw) & 1023u)) & 1023u);
+  unsigned char *awts = bwin + (size_t)R * P::kBBytes;
+  TcTilt *tab = (TcTilt *)(awts + (size_t)R * kABytes);
+  TcGroup *gtab = (TcGroup *)(tab + kTcMaxTilts);
 
   const int ntx = (a.X + kTX - 1) / kTX;
   const int x0 = (blockIdx.x % ntx) * kTX, z0 = (blockIdx.x / ntx) * kTZ;
@@ -225,11 +229,11 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
   if (warp == kWarpMma) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      sa(&tmem_base)),
-                 "r"((unsigned)kTmemCols));
+                 "r"((unsigned)P::kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    for (int i = 0; i < kS; ++i) {
+    for (int i = 0; i < kSB; ++i) {
       bar_init(&full[i], kBuilders + 1);
       bar_init(&empty[i], 1);
     }
@@ -271,38 +275,75 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
     tt.cos_a = g.cos_a;
     tt.sin_a = g.sin_a;
     tt.off = off;
-    tt.pad = 0.f;
+    tt.slot = 0;
     tab[t] = tt;
     atomicMin(&s_e0, (int)a.tilt_exp[t]);
+  }
+  __syncthreads();
+  const int e0 = s_e0;
+  for (int t = tid; t < a.T; t += kThreads) tab[t].wfac = pow2f(max(-126, e0 - (int)a.tilt_exp[t]));
+  if (warp == 0) {  // running slot counts: an exclusive prefix sum of nk over the tilts
+    const int chunk = (a.T + 31) / 32, t0 = lane * chunk, t1 = min(a.T, t0 + chunk);
+    int local = 0;
+    for (int t = t0; t < t1; ++t) local += tab[t].nk;
+    int incl = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    int run = incl - local;
+    for (int t = t0; t < t1; ++t) {
+      tab[t].slot = run;
+      run += tab[t].nk;
+    }
+  }
+  __syncthreads();
+  for (int g = tid; g < ngroups; g += kThreads) {
+    int n = 0;
+    for (int j = 0; j < kG && g * kG + j < a.T; ++j) n += tab[g * kG + j].nk;
+    gtab[g].c = tab[g * kG].slot;
+    gtab[g].n = n;
+  }
+  __syncthreads();
+  // the group that last used a slot of group g: the one holding running slot
+  // c + n - 1 - R (the groups' slots are consecutive)
+  for (int g = tid; g < ngroups; g += kThreads) {
+    const int target = gtab[g].c + gtab[g].n - 1 - R;
+    int w = -1;
+    if (target >= 0) {
+      int lo = 0, hi = g - 1;  // largest group whose first slot is <= target
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (gtab[mid].c <= target) lo = mid; else hi = mid - 1;
+      }
+      w = lo;
+    }
+    gtab[g].w = w;
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  const int e0 = s_e0;
-  for (int t = tid; t < a.T; t += kThreads) tab[t].wfac = pow2f(max(-126, e0 - (int)a.tilt_exp[t]));
-  __syncthreads();
   const unsigned tmem = tmem_base;
 
   if (warp == kWarpTma) {
-    // ---- TMA producer: group g's windows into stage g % kS
+    // ---- TMA producer: each slab's window into its slot
     if (lane == 0) {
       const int yrow = a.y_begin + y0;
       for (int g = 0; g < ngroups; ++g) {
-        const int st = g % kS;
-        bar_wait(&empty[st], ((g / kS) & 1) ^ 1, limit, a.err);
-        unsigned bytes = 0;
-        for (int j = 0; j < kG && g * kG + j < a.T; ++j) bytes += tab[g * kG + j].nk * P::kSlabBytes;
-        bar_expect_tx(&full[st], bytes);  // the producer's arrival, with the bytes to come
+        const TcGroup gr = gtab[g];
+        if (gr.w >= 0) bar_wait(&empty[gr.w % kSB], (gr.w / kSB) & 1, limit, a.err);
+        bar_expect_tx(&full[g % kSB], (unsigned)(gr.n * P::kBBytes));
         for (int j = 0; j < kG && g * kG + j < a.T; ++j) {
           const int i = g * kG + j;
           const TcTilt tt = tab[i];
           for (int s = 0; s < tt.nk; ++s) {
-            const unsigned dst =
-                sa(win + (size_t)st * P::kStageBytes + (size_t)(j * KMAX + s) * P::kSlabBytes);
+            const int slot = (tt.slot + s) % R;
             asm volatile(
                 "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes "
-                "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
-                "l"(&map), "r"(tt.u0), "r"(yrow), "r"((tt.k0 + s) * a.T + i), "r"(sa(&full[st]))
+                "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(sa(bwin + (size_t)slot * P::kBBytes)),
+                "l"(&map), "r"(tt.u0), "r"(yrow), "r"((tt.k0 + s) * a.T + i),
+                "r"(sa(&full[g % kSB]))
                 : "memory");
           }
         }
@@ -312,38 +353,37 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
     // ---- MMA issuer: one wait and one commit per group
     if (lane == 0) {
       for (int g = 0; g < ngroups; ++g) {
-        const int st = g % kS;
-        bar_wait(&full[st], (g / kS) & 1, limit, a.err);
+        bar_wait(&full[g % kSB], (g / kSB) & 1, limit, a.err);
         tc_fence_after();
-        const unsigned wbase = sa(win + (size_t)st * P::kStageBytes);
-        const unsigned abase = tmem + NR + st * P::kACols;
         for (int j = 0; j < kG && g * kG + j < a.T; ++j) {
-          const int nk = tab[g * kG + j].nk;
-          for (int s = 0; s < nk; ++s)
+          const TcTilt tt = tab[g * kG + j];
+          for (int s = 0; s < tt.nk; ++s) {
+            const int slot = (tt.slot + s) % R;
+            const unsigned ab = sa(awts + (size_t)slot * kABytes);
+            const unsigned bb = sa(bwin + (size_t)slot * P::kBBytes);
             for (int kk = 0; kk < 2; ++kk)
-              mma(tmem, abase + (j * KMAX + s) * (kKW / 2) + kk * 8,
-                  b_desc(wbase + (j * KMAX + s) * P::kSlabBytes + kk * 32), P::kIdesc,
+              mma(tmem, a_desc(ab + kk * 2 * kAChunk), b_desc(bb + kk * 32), P::kIdesc,
                   (g | j | s | kk) != 0 ? 1u : 0u);
+          }
         }
-        mma_commit(&empty[st]);  // the stage is free once these MMAs complete
+        mma_commit(&empty[g % kSB]);  // the group's slots are free once these complete
       }
       mma_commit(&done_bar);
     }
   } else {
-    // ---- weight builders: voxel m = (x0 + m % 16, z0 + m / 16) = tensor-memory
-    // lane m; this thread writes part h of the window (pixels kKW / kQ h ..,
-    // columns kKW / 2 / kQ h .. of each slab's block)
+    // ---- weight builders: voxel m = (x0 + m % 16, z0 + m / 16) = MMA row m;
+    // this thread writes pixels 16 h .. 16 h + 15 of the voxel's weight rows
     const int m = 32 * (warp & 3) + lane, h = warp >> 2;
     const int x = x0 + (m & (kTX - 1)), z = z0 + (m >> 4);
     const bool inside = x < a.X && z < a.Z;
     const float xf = voxel_coordf(x, a.X), zf = voxel_coordf(z, a.Z);
-    const unsigned lane_addr = (unsigned)(32 * (warp & 3)) << 16;
+    // byte offset of (voxel m, pixel 8 c) in a weight block: 8 x 16-byte core matrices
+    const unsigned roff = (unsigned)((m >> 3) * 128 + (m & 7) * 16);
     for (int g = 0; g < ngroups; ++g) {
-      const int st = g % kS;
       // the group's weights first (independent tilts: their arithmetic
-      // interleaves), then the wait for the stage
-      unsigned lo[kG], hi[kG];
-      int idx[kG], blk[kG];
+      // interleaves), then the wait for its slots
+      unsigned short h0[kG], h1[kG];
+      int pos[kG], blk[kG];
 #pragma unroll
       for (int j = 0; j < kG; ++j) {
         const int i = min(g * kG + j, a.T - 1);
@@ -354,49 +394,49 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
         const float tw = __fsub_rn(q, __fsub_rn(r, kMagic));
         const int k = tt.nk > 1 ? slab_index(xf, zf, tt.sin_a, tt.cos_a, a.dscale, a.doffset, a.D)
                                 : tt.k0;
-        const int pos = fl - tt.u0;
+        pos[j] = fl - tt.u0;
         // the reference skips samples unless 0 <= floor <= N - 2
         bool valid = inside && fl >= 0 && fl <= a.N - 2;
-        if (valid && (pos < 0 || pos > kKW - 2)) {  // excluded by the tile's window
+        if (valid && (pos[j] < 0 || pos[j] > kKW - 2)) {  // excluded by the tile's window
           valid = false;
           if (a.err) atomicOr(a.err, 4);
         }
-        const unsigned h0 =
-            __half_as_ushort(__float2half_rn(__fmul_rn(__fsub_rn(1.f, tw), tt.wfac)));
-        const unsigned h1 = __half_as_ushort(__float2half_rn(__fmul_rn(tw, tt.wfac)));
-        const u64 pair = (u64)(h0 | (h1 << 16)) << ((pos & 1) * 16);
-        lo[j] = (unsigned)pair;
-        hi[j] = (unsigned)(pair >> 32);
-        idx[j] = (pos >> 1) - kWords * h;       // word of this part holding the pixel pair
-        blk[j] = valid ? k - tt.k0 : -1;        // the slab block holding the weights
+        h0[j] = __half_as_ushort(__float2half_rn(__fmul_rn(__fsub_rn(1.f, tw), tt.wfac)));
+        h1[j] = __half_as_ushort(__float2half_rn(__fmul_rn(tw, tt.wfac)));
+        blk[j] = valid ? k - tt.k0 : -1;  // the slab block holding the weights
       }
-      bar_wait(&empty[st], ((g / kS) & 1) ^ 1, limit, a.err);
-      tc_fence_after();
-      const unsigned abase = tmem + lane_addr + NR + st * P::kACols + kWords * h;
+      const TcGroup gr = gtab[g];
+      if (gr.w >= 0) bar_wait(&empty[gr.w % kSB], (gr.w / kSB) & 1, limit, a.err);
 #pragma unroll
       for (int j = 0; j < kG; ++j) {
         if (g * kG + j >= a.T) break;
-        const int nk = tab[g * kG + j].nk;
+        const TcTilt tt = tab[g * kG + j];
 #pragma unroll
         for (int s = 0; s < KMAX; ++s) {
-          if (s < nk) {
-            const bool mine = blk[j] == s;
-            unsigned w[kWords];
-#pragma unroll
-            for (int q = 0; q < kWords; ++q)
-              w[q] = !mine ? 0u : (q == idx[j] ? lo[j] : (q == idx[j] + 1 ? hi[j] : 0u));
-            tmem_st(abase + (j * KMAX + s) * (kKW / 2), w);
+          if (s < tt.nk) {
+            unsigned char *blkp = awts + (size_t)((tt.slot + s) % R) * kABytes + roff;
+            // this half of the row to zero, then the voxel's two weights
+            *(uint4 *)(blkp + (2 * h) * kAChunk) = make_uint4(0, 0, 0, 0);
+            *(uint4 *)(blkp + (2 * h + 1) * kAChunk) = make_uint4(0, 0, 0, 0);
+            if (blk[j] == s) {
+              const int p0 = pos[j], p1 = pos[j] + 1;
+              if ((p0 >> 4) == h)
+                *(unsigned short *)(blkp + (p0 >> 3) * kAChunk + (p0 & 7) * 2) = h0[j];
+              if ((p1 >> 4) == h)
+                *(unsigned short *)(blkp + (p1 >> 3) * kAChunk + (p1 & 7) * 2) = h1[j];
+            }
           }
         }
       }
-      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-      tc_fence_before();
-      bar_arrive(&full[st]);
+      // the tensor cores read the weights through the async proxy
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      bar_arrive(&full[g % kSB]);
     }
     // ---- store: the accumulator of voxel m; this thread's half of the rows
     bar_wait(&done_bar, 0, limit, a.err);
     tc_fence_after();
     const float sc = a.geom[0].scale * pow2f(max(-126, min(127, -e0)));
+    const unsigned lane_addr = (unsigned)(32 * (warp & 3)) << 16;
 #pragma unroll 1
     for (int c = h * (NR / kQ); c < (h + 1) * (NR / kQ); c += 32) {
       unsigned v[32];
@@ -414,7 +454,7 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
   __syncthreads();
   if (warp == kWarpMma)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                 "r"((unsigned)kTmemCols));
+                 "r"((unsigned)P::kTmemCols));
 }
 
 // Sum of squares of each input tilt in kTiltPartsMax partial sums (float: the
@@ -494,7 +534,7 @@ bool backproject_tc_supported(int N, int T, float dscale, int D, bool uniform_ce
 }
 
 // Rows per block of the shape a geometry uses (the TMA box height).
-constexpr int kRowsTwoSlabs = 128;
+constexpr int kRowsTwoSlabs = 256;
 int tc_rows(float dscale, int D) { return tc_slabs_per_tile(dscale, D) <= 2 ? kRowsTwoSlabs : 128; }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
@@ -531,12 +571,11 @@ cudaError_t make_tc_map(const void *staged, int D, int T, int H, int N, int rows
   return cudaSuccess;
 }
 
-template <int NR, int KMAX, int S, int TMEM, int BLOCKS>
+template <int NR, int KMAX, int R>
 static cudaError_t launch_tc(const BpArgs &a, const TcMap &map, cudaStream_t s) {
-  using P = TcShape<NR, KMAX, S, TMEM, BLOCKS>;
-  auto kern = k_bp_tc<NR, KMAX, S, TMEM, BLOCKS>;
-  if (cudaError_t e = ensure_dynamic_smem<k_bp_tc<NR, KMAX, S, TMEM, BLOCKS>>((int)P::kSmem))
-    return e;
+  using P = TcShape<NR, KMAX, R>;
+  auto kern = k_bp_tc<NR, KMAX, R>;
+  if (cudaError_t e = ensure_dynamic_smem<k_bp_tc<NR, KMAX, R>>((int)P::kSmem)) return e;
   const int ntx = (a.X + kTX - 1) / kTX, ntz = (a.Z + kTZ - 1) / kTZ;
   dim3 grid(ntx * ntz, (a.Y + NR - 1) / NR);
   CUtensorMap m;
@@ -548,13 +587,8 @@ static cudaError_t launch_tc(const BpArgs &a, const TcMap &map, cudaStream_t s) 
 cudaError_t launch_backproject_tc(const BpArgs &a, const TcMap &map, cudaStream_t s) {
   // the map's box height is the shape's row count
   if (map.rows != tc_rows(a.dscale, a.D)) return cudaErrorInvalidValue;
-  // up to two slabs per tile: 256 rows, one block per SM, or 128 rows, two
-  // blocks per SM (one block's set-up and volume stores overlap the other's
-  // tilt loop); three slabs: 128 rows, one block per SM
-  if (tc_slabs_per_tile(a.dscale, a.D) <= 2)
-    return map.rows == 256 ? launch_tc<256, 2, 3, 512, 1>(a, map, s)
-                           : launch_tc<128, 2, 2, 256, 2>(a, map, s);
-  return launch_tc<128, 3, 3, 512, 1>(a, map, s);
+  // up to two slabs per tile: 256 rows, 8 slots; three: 128 rows, 12 slots
+  return map.rows == 256 ? launch_tc<256, 2, 8>(a, map, s) : launch_tc<128, 3, 12>(a, map, s);
 }
 
 }  // namespace gnc
