@@ -28,25 +28,37 @@
 // bit for bit (as in gnc_bp.cu); the products and sums are FP16 x FP16 -> FP32
 // on the tensor cores.
 //
-// Warp roles (320 threads, one block per SM): warps 0-7 build weights
-// (warps w and w + 4 the two window halves of voxels 32 (w % 4) ..) and store
-// the volume, warp 8 issues the TMA loads, warp 9 owns the tensor memory and
-// issues the MMAs.  Tilts go in groups of kG, each with a "full" mbarrier
-// (the builders and the producer arrive, the windows' bytes complete it) and
-// an "empty" one (the MMAs' commit); a group's slots are consecutive in the
-// ring, so before filling them the producer and the builders wait for the
-// one earlier group that last used the newest of them (a per-group table
-// built once per block from the tilts' slab counts).  The builders compute a
-// group's weights before that wait and read the tilts' geometry from a
-// shared-memory table.  Measured on the 61-tilt 1024 x 1024 x 300 ten-slab
-// series: weights in tensor memory (tcgen05.st of all 32 words per voxel)
-// 2.41 ms, weights in shared memory with two 16-byte zero stores and two
-// 2-byte weight stores per thread and slot 2.17 ms.  (Prefetching the windows
-// of later tilts into L2 made the kernel 25 % slower: the prefetches compete
-// with the loads.)  Every wait is bounded and records a timeout in the plan's
-// error word.
+// The kernel is persistent: one block per SM (its shared memory allows no
+// second) takes tiles b, b + gridDim.x, ...; its j-th tile accumulates into
+// accumulator j % 2 of tensor memory (2 x NR columns) and reads table buffer
+// j % 2, so the next tile's table is built and the last tile's accumulator is
+// stored while the current tile runs.  Warp roles (448 threads): warps 0-7
+// build weights (warps w and w + 4 the two window halves of voxels 32 (w % 4)
+// ..), warp 8 issues the TMA loads, warp 9 owns the tensor memory and issues
+// the MMAs, warps 10-13 build each tile's tilt and group tables and store the
+// accumulators.  Tilts go in groups of kG, each with a "full" mbarrier (the
+// builders and the producer arrive, the windows' bytes complete it) and an
+// "empty" one (the MMAs' commit); group numbers and slot counts run on across
+// a block's tiles.  A group's slots are consecutive in the ring, so before
+// filling them the producer and the builders wait for the one earlier group
+// that last used the newest of them, found when the table is built.  The
+// builders compute a group's weights before that wait.
+//
+// Measured on the 61-tilt 1024 x 1024 x 300 ten-slab series (GB300): weights
+// in tensor memory (tcgen05.st of all 32 words per voxel) 2.41 ms; weights in
+// shared memory, two 16-byte zero stores and two 2-byte weight stores per
+// thread and slot, 2.17 ms; persistent with the table and store overlapped
+// 1.69 ms.  Clock stamps of the non-persistent form put 39 % of a block's time
+// outside the group loop (table 8 %, pipeline fill 7 %, drain 5 %, volume
+// stores 19 %), and inside it a group period of ~1400 cycles against ~990 of
+// MMA issue: shared memory bandwidth (window writes, operand reads, weight
+// stores) is the loop's bound.  Prefetching the windows of later tilts into
+// L2 made the kernel 25 % slower (the prefetches compete with the loads).
+// Every wait is bounded and records a timeout in the plan's error word; after
+// one timeout the block's remaining waits return at once.
 #include <cuda.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -61,9 +73,10 @@ constexpr int kKW = 32;           // window pixels (two K = 16 steps)
 constexpr int kG = 2;             // tilts per group: one barrier round trip per group
 constexpr int kQ = 2;             // builder threads per voxel (window halves)
 constexpr int kBuilders = 128 * kQ;       // warps 0-7
-constexpr int kThreads = kBuilders + 64;  // + TMA warp + MMA warp
-constexpr int kWarpTma = kBuilders / 32, kWarpMma = kWarpTma + 1;
-constexpr int kSB = 8;            // barrier stages (more than the groups in flight)
+constexpr int kEpi = 128;                 // table and store threads: warps 10-13
+constexpr int kThreads = kBuilders + 64 + kEpi;
+constexpr int kWarpTma = kBuilders / 32, kWarpMma = kWarpTma + 1, kWarpEpi = kWarpMma + 1;
+constexpr int kSB = 16;           // group barrier stages (more than the groups in flight)
 constexpr unsigned kHintNs = 1000;
 constexpr int kABytes = 128 * kKW * 2;  // one slab's weights: 128 voxels x 32 pixels, FP16
 constexpr int kAChunk = 128 * 16;       // 8 pixels of all 128 voxels (one K core-matrix column)
@@ -73,11 +86,14 @@ constexpr int kAChunk = 128 * 16;       // 8 pixels of all 128 voxels (one K cor
 template <int NR, int KMAX, int R>
 struct TcShape {
   static constexpr int kBBytes = NR * kKW * 2;  // one slab's window: NR rows x 32 pixels
-  static constexpr int kTmemCols = NR;          // the accumulator only
+  static constexpr int kTmemCols = 2 * NR;      // two accumulators (tile j in j % 2)
   static_assert(R >= 2 * kG * KMAX, "a slot ring holds two groups");
-  static_assert(R / 2 + 1 < kSB, "waits reach back fewer groups than barrier stages");
+  // a group waits for a group at most R groups back (every group has a slot)
+  static_assert(R < kSB, "waits reach back fewer groups than barrier stages");
+  // per tile buffer: the tilt table and the group table
+  static constexpr size_t kTabBytes = (size_t)kTcMaxTilts * 16 + (size_t)(kTcMaxTilts / kG) * 16;
   static constexpr size_t kSmem = 1024 + (size_t)R * (kBBytes + kABytes) +
-                                  (size_t)kTcMaxTilts * 32 + (size_t)(kTcMaxTilts / kG) * 16;
+                                  (size_t)kTcMaxTilts * 16 + 2 * kTabBytes;
   static_assert(kSmem <= 227 * 1024, "shared memory");
   static constexpr unsigned kIdesc = (1u << 4) | ((unsigned)(NR >> 3) << 17) | ((128u >> 4) << 24);
 };
@@ -87,14 +103,15 @@ constexpr int kMagicBits = 0x4B400000;
 
 typedef unsigned long long u64;
 
+// One tilt over one tile.
 struct TcTilt {
   int u0;      // first window pixel (multiple of 8; may be negative)
   int k0, nk;  // first slab and slab count of the tile
-  float wfac;  // 2^(E0 - e(t))
-  float cos_a, sin_a, off;  // the tilt's geometry (reconstructor.cpp:35-47)
-  int slot;    // running slot count of its first slab (slot slot % R)
+  int slot;    // the block's running slot count at its first slab (ring slot slot % R)
 };
 
+// One group of kG tilts over one tile; group and slot counts run on over the
+// block's tiles.
 struct TcGroup {
   int c, n;    // first running slot and slot count of the group
   int w;       // the last earlier group that used one of these slots (-1: none)
@@ -125,21 +142,34 @@ __device__ __forceinline__ void bar_expect_tx(u64 *b, unsigned bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sa(b)), "r"(bytes)
                : "memory");
 }
-// Bounded wait for the phase of the given parity; false (and the error word
-// set) if it did not complete within `limit` polls.
-__device__ __forceinline__ bool bar_wait(u64 *b, unsigned parity, unsigned limit, int *err) {
+__device__ __forceinline__ bool bar_try(u64 *b, unsigned parity) {
+  unsigned done;
+  asm volatile(
+      "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3; "
+      "selp.u32 %0, 1, 0, p; }"
+      : "=r"(done)
+      : "r"(sa(b)), "r"(parity), "r"(kHintNs)
+      : "memory");
+  return done != 0;
+}
+// Bounded wait for the phase of the given parity.  If it does not complete
+// within `limit` polls the error word and the block's abort flag are set and
+// it returns false; once the flag is set every wait returns at once, so a
+// broken pipeline ends the kernel after one timeout instead of one per wait.
+__device__ __forceinline__ bool bar_wait(u64 *b, unsigned parity, unsigned limit, int *err,
+                                         volatile int *abort) {
   for (unsigned it = 0; it < limit; ++it) {
-    unsigned done;
-    asm volatile(
-        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3; "
-        "selp.u32 %0, 1, 0, p; }"
-        : "=r"(done)
-        : "r"(sa(b)), "r"(parity), "r"(kHintNs)
-        : "memory");
-    if (done) return true;
+    if (bar_try(b, parity)) return true;
+    if (*abort) return false;
   }
+  *abort = 1;
   if (err) atomicOr(err, 1);
   return false;
+}
+// Bounded wait that ignores the abort flag (for the block's final drain).
+__device__ __forceinline__ void bar_wait_plain(u64 *b, unsigned parity, unsigned limit) {
+  for (unsigned it = 0; it < limit && !bar_try(b, parity); ++it) {
+  }
 }
 
 __device__ __forceinline__ void tc_fence_before() {
@@ -198,6 +228,33 @@ __device__ __forceinline__ void tmem_ld32(unsigned taddr, unsigned (&v)[32]) {
 
 }  // namespace
 
+__device__ __forceinline__ void epi_sync() {  // the kEpi table and store threads
+  asm volatile("bar.sync 1, %0;" ::"n"(kEpi) : "memory");
+}
+
+// Largest index i in [lo, hi] with gt[i].c <= target (gt[lo].c <= target).
+__device__ __forceinline__ int last_group_at(const TcGroup *gt, int lo, int hi, int target) {
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (gt[mid].c <= target) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+struct TcTile {
+  int x0, z0, y0;
+};
+__device__ __forceinline__ TcTile tc_tile(int tile, int ntx, int ntz, int nr) {
+  TcTile t;
+  t.x0 = (tile % ntx) * kTX;
+  t.z0 = ((tile / ntx) % ntz) * kTZ;
+  t.y0 = (tile / (ntx * ntz)) * nr;
+  return t;
+}
+
+// Persistent: block b takes tiles b, b + gridDim.x, ...  Its j-th tile uses
+// accumulator j % 2 and table buffer j % 2; group barriers run on across the
+// tiles (the j-th tile's group g is the block's group j * ngroups + g).
 template <int NR, int KMAX, int R>
 __global__ void __launch_bounds__(kThreads, 1)
 k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
@@ -207,23 +264,31 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
     a.doffset = a.dyn[1];
   }
   extern __shared__ unsigned char smem_raw[];
-  // full[g % kSB]: the builders and the TMA producer arrive (plus the windows'
-  // bytes); empty[g % kSB]: the MMAs of group g have completed
-  __shared__ __align__(8) u64 full[kSB], empty[kSB], done_bar;
+  // full[G % kSB]: the builders and the TMA producer arrive (plus the windows'
+  // bytes); empty[G % kSB]: the MMAs of group G have completed.  acc_full[b]:
+  // a tile's MMAs into accumulator b have completed; acc_empty[b]: the store
+  // threads have read it.  tab_full[b]: table buffer b is written; tab_empty[b]:
+  // the producer, the MMA issuer and the builders are done with it.
+  __shared__ __align__(8) u64 full[kSB], empty[kSB], acc_full[2], acc_empty[2], tab_full[2],
+      tab_empty[2], done_bar;
   __shared__ unsigned tmem_base;
   __shared__ int s_e0;
+  __shared__ volatile int s_abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const unsigned limit = a.wait_limit ? a.wait_limit : kBpWaitLimit;
   // 1024-aligned windows (the 64-byte swizzle repeats every 512 bytes), then
-  // the weight blocks, the tilt table and the group table
+  // the weight blocks, the tilts' constants and the two table buffers
   unsigned char *bwin = smem_raw + ((1024u - (sa(smem_raw) & 1023u)) & 1023u);
   unsigned char *awts = bwin + (size_t)R * P::kBBytes;
-  TcTilt *tab = (TcTilt *)(awts + (size_t)R * kABytes);
-  TcGroup *gtab = (TcGroup *)(tab + kTcMaxTilts);
+  float4 *tconst = (float4 *)(awts + (size_t)R * kABytes);  // cos, sin, offset, 2^(E0 - e(t))
+  unsigned char *tabs = (unsigned char *)(tconst + kTcMaxTilts);
+  auto tilt_tab = [&](int b) { return (TcTilt *)(tabs + b * P::kTabBytes); };
+  auto group_tab = [&](int b) {
+    return (TcGroup *)(tabs + b * P::kTabBytes + (size_t)kTcMaxTilts * 16);
+  };
 
-  const int ntx = (a.X + kTX - 1) / kTX;
-  const int x0 = (blockIdx.x % ntx) * kTX, z0 = (blockIdx.x / ntx) * kTZ;
-  const int y0 = blockIdx.y * NR;
+  const int ntx = (a.X + kTX - 1) / kTX, ntz = (a.Z + kTZ - 1) / kTZ;
+  const int ntiles = ntx * ntz * ((a.Y + NR - 1) / NR);
   const int ngroups = (a.T + kG - 1) / kG;
 
   if (warp == kWarpMma) {
@@ -237,89 +302,25 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
       bar_init(&full[i], kBuilders + 1);
       bar_init(&empty[i], 1);
     }
+    for (int b = 0; b < 2; ++b) {
+      bar_init(&acc_full[b], 1);
+      bar_init(&acc_empty[b], kEpi);
+      bar_init(&tab_full[b], kEpi);
+      bar_init(&tab_empty[b], kBuilders + 2);
+    }
     bar_init(&done_bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     s_e0 = 127;
+    s_abort = 0;
   }
   __syncthreads();
-  // the tile's window and slabs per tilt: corners inside the volume (the
-  // coordinate and the slab index are monotone in x and in z)
-  const float cx0 = voxel_coordf(x0, a.X), cx1 = voxel_coordf(min(x0 + kTX, a.X) - 1, a.X);
-  const float cz0 = voxel_coordf(z0, a.Z), cz1 = voxel_coordf(min(z0 + kTZ, a.Z) - 1, a.Z);
-  for (int t = tid; t < a.T; t += kThreads) {
-    const TiltGeom g = a.geom[t];
-    const float off = a.offset[t];
-    const float xc0 = __fmul_rn(cx0, g.cos_a), xc1 = __fmul_rn(cx1, g.cos_a);
-    const float zs0 = __fmul_rn(cz0, g.sin_a), zs1 = __fmul_rn(cz1, g.sin_a);
-    const float q00 = detector_coord(xc0, zs0, off), q01 = detector_coord(xc0, zs1, off);
-    const float q10 = detector_coord(xc1, zs0, off), q11 = detector_coord(xc1, zs1, off);
-    const int p_lo = floor_int(fminf(fminf(q00, q01), fminf(q10, q11)));
-    int k_lo = 0, k_hi = 0;
-    if (a.D > 1) {
-      const int k00 = slab_index(cx0, cz0, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
-      const int k01 = slab_index(cx0, cz1, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
-      const int k10 = slab_index(cx1, cz0, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
-      const int k11 = slab_index(cx1, cz1, g.sin_a, g.cos_a, a.dscale, a.doffset, a.D);
-      k_lo = min(min(k00, k01), min(k10, k11));
-      k_hi = max(max(k00, k01), max(k10, k11));
-    }
-    TcTilt tt;
-    tt.u0 = p_lo & ~7;  // round down to a multiple of 8 (also for negative p_lo)
-    tt.k0 = k_lo;
-    tt.nk = k_hi - k_lo + 1;
-    if (tt.nk > KMAX) {  // excluded by the host's choice of shape
-      tt.nk = KMAX;
-      if (a.err) atomicOr(a.err, 2);
-    }
-    tt.wfac = 0.f;
-    tt.cos_a = g.cos_a;
-    tt.sin_a = g.sin_a;
-    tt.off = off;
-    tt.slot = 0;
-    tab[t] = tt;
-    atomicMin(&s_e0, (int)a.tilt_exp[t]);
-  }
+  for (int t = tid; t < a.T; t += kThreads) atomicMin(&s_e0, (int)a.tilt_exp[t]);
   __syncthreads();
   const int e0 = s_e0;
-  for (int t = tid; t < a.T; t += kThreads) tab[t].wfac = pow2f(max(-126, e0 - (int)a.tilt_exp[t]));
-  if (warp == 0) {  // running slot counts: an exclusive prefix sum of nk over the tilts
-    const int chunk = (a.T + 31) / 32, t0 = lane * chunk, t1 = min(a.T, t0 + chunk);
-    int local = 0;
-    for (int t = t0; t < t1; ++t) local += tab[t].nk;
-    int incl = local;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int v = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += v;
-    }
-    int run = incl - local;
-    for (int t = t0; t < t1; ++t) {
-      tab[t].slot = run;
-      run += tab[t].nk;
-    }
-  }
-  __syncthreads();
-  for (int g = tid; g < ngroups; g += kThreads) {
-    int n = 0;
-    for (int j = 0; j < kG && g * kG + j < a.T; ++j) n += tab[g * kG + j].nk;
-    gtab[g].c = tab[g * kG].slot;
-    gtab[g].n = n;
-  }
-  __syncthreads();
-  // the group that last used a slot of group g: the one holding running slot
-  // c + n - 1 - R (the groups' slots are consecutive)
-  for (int g = tid; g < ngroups; g += kThreads) {
-    const int target = gtab[g].c + gtab[g].n - 1 - R;
-    int w = -1;
-    if (target >= 0) {
-      int lo = 0, hi = g - 1;  // largest group whose first slot is <= target
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (gtab[mid].c <= target) lo = mid; else hi = mid - 1;
-      }
-      w = lo;
-    }
-    gtab[g].w = w;
+  for (int t = tid; t < a.T; t += kThreads) {
+    const TiltGeom g = a.geom[t];
+    tconst[t] = make_float4(g.cos_a, g.sin_a, a.offset[t],
+                            pow2f(max(-126, e0 - (int)a.tilt_exp[t])));
   }
   tc_fence_before();
   __syncthreads();
@@ -329,126 +330,262 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
   if (warp == kWarpTma) {
     // ---- TMA producer: each slab's window into its slot
     if (lane == 0) {
-      const int yrow = a.y_begin + y0;
-      for (int g = 0; g < ngroups; ++g) {
-        const TcGroup gr = gtab[g];
-        if (gr.w >= 0) bar_wait(&empty[gr.w % kSB], (gr.w / kSB) & 1, limit, a.err);
-        bar_expect_tx(&full[g % kSB], (unsigned)(gr.n * P::kBBytes));
-        for (int j = 0; j < kG && g * kG + j < a.T; ++j) {
-          const int i = g * kG + j;
-          const TcTilt tt = tab[i];
-          for (int s = 0; s < tt.nk; ++s) {
-            const int slot = (tt.slot + s) % R;
-            asm volatile(
-                "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes "
-                "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(sa(bwin + (size_t)slot * P::kBBytes)),
-                "l"(&map), "r"(tt.u0), "r"(yrow), "r"((tt.k0 + s) * a.T + i),
-                "r"(sa(&full[g % kSB]))
-                : "memory");
-          }
-        }
-      }
-    }
-  } else if (warp == kWarpMma) {
-    // ---- MMA issuer: one wait and one commit per group
-    if (lane == 0) {
-      for (int g = 0; g < ngroups; ++g) {
-        bar_wait(&full[g % kSB], (g / kSB) & 1, limit, a.err);
-        tc_fence_after();
-        for (int j = 0; j < kG && g * kG + j < a.T; ++j) {
-          const TcTilt tt = tab[g * kG + j];
-          for (int s = 0; s < tt.nk; ++s) {
-            const int slot = (tt.slot + s) % R;
-            const unsigned ab = sa(awts + (size_t)slot * kABytes);
-            const unsigned bb = sa(bwin + (size_t)slot * P::kBBytes);
-            for (int kk = 0; kk < 2; ++kk)
-              mma(tmem, a_desc(ab + kk * 2 * kAChunk), b_desc(bb + kk * 32), P::kIdesc,
-                  (g | j | s | kk) != 0 ? 1u : 0u);
-          }
-        }
-        mma_commit(&empty[g % kSB]);  // the group's slots are free once these complete
-      }
-      mma_commit(&done_bar);
-    }
-  } else {
-    // ---- weight builders: voxel m = (x0 + m % 16, z0 + m / 16) = MMA row m;
-    // this thread writes pixels 16 h .. 16 h + 15 of the voxel's weight rows
-    const int m = 32 * (warp & 3) + lane, h = warp >> 2;
-    const int x = x0 + (m & (kTX - 1)), z = z0 + (m >> 4);
-    const bool inside = x < a.X && z < a.Z;
-    const float xf = voxel_coordf(x, a.X), zf = voxel_coordf(z, a.Z);
-    // byte offset of (voxel m, pixel 8 c) in a weight block: 8 x 16-byte core matrices
-    const unsigned roff = (unsigned)((m >> 3) * 128 + (m & 7) * 16);
-    for (int g = 0; g < ngroups; ++g) {
-      // the group's weights first (independent tilts: their arithmetic
-      // interleaves), then the wait for its slots
-      unsigned short h0[kG], h1[kG];
-      int pos[kG], blk[kG];
-#pragma unroll
-      for (int j = 0; j < kG; ++j) {
-        const int i = min(g * kG + j, a.T - 1);
-        const TcTilt tt = tab[i];
-        const float q = detector_coord(__fmul_rn(xf, tt.cos_a), __fmul_rn(zf, tt.sin_a), tt.off);
-        const float r = __fadd_rd(q, kMagic);
-        const int fl = __float_as_int(r) - kMagicBits;
-        const float tw = __fsub_rn(q, __fsub_rn(r, kMagic));
-        const int k = tt.nk > 1 ? slab_index(xf, zf, tt.sin_a, tt.cos_a, a.dscale, a.doffset, a.D)
-                                : tt.k0;
-        pos[j] = fl - tt.u0;
-        // the reference skips samples unless 0 <= floor <= N - 2
-        bool valid = inside && fl >= 0 && fl <= a.N - 2;
-        if (valid && (pos[j] < 0 || pos[j] > kKW - 2)) {  // excluded by the tile's window
-          valid = false;
-          if (a.err) atomicOr(a.err, 4);
-        }
-        h0[j] = __half_as_ushort(__float2half_rn(__fmul_rn(__fsub_rn(1.f, tw), tt.wfac)));
-        h1[j] = __half_as_ushort(__float2half_rn(__fmul_rn(tw, tt.wfac)));
-        blk[j] = valid ? k - tt.k0 : -1;  // the slab block holding the weights
-      }
-      const TcGroup gr = gtab[g];
-      if (gr.w >= 0) bar_wait(&empty[gr.w % kSB], (gr.w / kSB) & 1, limit, a.err);
-#pragma unroll
-      for (int j = 0; j < kG; ++j) {
-        if (g * kG + j >= a.T) break;
-        const TcTilt tt = tab[g * kG + j];
-#pragma unroll
-        for (int s = 0; s < KMAX; ++s) {
-          if (s < tt.nk) {
-            unsigned char *blkp = awts + (size_t)((tt.slot + s) % R) * kABytes + roff;
-            // this half of the row to zero, then the voxel's two weights
-            *(uint4 *)(blkp + (2 * h) * kAChunk) = make_uint4(0, 0, 0, 0);
-            *(uint4 *)(blkp + (2 * h + 1) * kAChunk) = make_uint4(0, 0, 0, 0);
-            if (blk[j] == s) {
-              const int p0 = pos[j], p1 = pos[j] + 1;
-              if ((p0 >> 4) == h)
-                *(unsigned short *)(blkp + (p0 >> 3) * kAChunk + (p0 & 7) * 2) = h0[j];
-              if ((p1 >> 4) == h)
-                *(unsigned short *)(blkp + (p1 >> 3) * kAChunk + (p1 & 7) * 2) = h1[j];
+      for (int j = 0, tile = blockIdx.x; tile < ntiles; ++j, tile += gridDim.x) {
+        const int b = j & 1;
+        bar_wait(&tab_full[b], (j >> 1) & 1, limit, a.err, &s_abort);
+        const TcTilt *tab = tilt_tab(b);
+        const TcGroup *gtab = group_tab(b);
+        const int yrow = a.y_begin + tc_tile(tile, ntx, ntz, NR).y0;
+        for (int g = 0; g < ngroups; ++g) {
+          const int G = j * ngroups + g;
+          const TcGroup gr = gtab[g];
+          if (gr.w >= 0) bar_wait(&empty[gr.w % kSB], (gr.w / kSB) & 1, limit, a.err, &s_abort);
+          bar_expect_tx(&full[G % kSB], (unsigned)(gr.n * P::kBBytes));
+          for (int jj = 0; jj < kG && g * kG + jj < a.T; ++jj) {
+            const int i = g * kG + jj;
+            const TcTilt tt = tab[i];
+            for (int sl = 0; sl < tt.nk; ++sl) {
+              const int slot = (tt.slot + sl) % R;
+              asm volatile(
+                  "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes "
+                  "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(sa(bwin + (size_t)slot * P::kBBytes)),
+                  "l"(&map), "r"(tt.u0), "r"(yrow), "r"((tt.k0 + sl) * a.T + i),
+                  "r"(sa(&full[G % kSB]))
+                  : "memory");
             }
           }
         }
+        bar_arrive(&tab_empty[b]);
       }
-      // the tensor cores read the weights through the async proxy
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      bar_arrive(&full[g % kSB]);
     }
-    // ---- store: the accumulator of voxel m; this thread's half of the rows
-    bar_wait(&done_bar, 0, limit, a.err);
-    tc_fence_after();
-    const float sc = a.geom[0].scale * pow2f(max(-126, min(127, -e0)));
-    const unsigned lane_addr = (unsigned)(32 * (warp & 3)) << 16;
-#pragma unroll 1
-    for (int c = h * (NR / kQ); c < (h + 1) * (NR / kQ); c += 32) {
-      unsigned v[32];
-      tmem_ld32(tmem + lane_addr + (unsigned)c, v);
-      if (inside) {
+  } else if (warp == kWarpMma) {
+    // ---- MMA issuer: one wait and one commit per group, accumulator j % 2
+    if (lane == 0) {
+      for (int j = 0, tile = blockIdx.x; tile < ntiles; ++j, tile += gridDim.x) {
+        const int b = j & 1;
+        bar_wait(&tab_full[b], (j >> 1) & 1, limit, a.err, &s_abort);
+        if (j >= 2) bar_wait(&acc_empty[b], ((j >> 1) - 1) & 1, limit, a.err, &s_abort);
+        tc_fence_after();
+        const TcTilt *tab = tilt_tab(b);
+        const unsigned d = tmem + (unsigned)(b * NR);
+        for (int g = 0; g < ngroups; ++g) {
+          const int G = j * ngroups + g;
+          bar_wait(&full[G % kSB], (G / kSB) & 1, limit, a.err, &s_abort);
+          tc_fence_after();
+          for (int jj = 0; jj < kG && g * kG + jj < a.T; ++jj) {
+            const TcTilt tt = tab[g * kG + jj];
+            for (int sl = 0; sl < tt.nk; ++sl) {
+              const int slot = (tt.slot + sl) % R;
+              const unsigned ab = sa(awts + (size_t)slot * kABytes);
+              const unsigned bb = sa(bwin + (size_t)slot * P::kBBytes);
+              for (int kk = 0; kk < 2; ++kk)
+                mma(d, a_desc(ab + kk * 2 * kAChunk), b_desc(bb + kk * 32), P::kIdesc,
+                    (g | jj | sl | kk) != 0 ? 1u : 0u);
+            }
+          }
+          mma_commit(&empty[G % kSB]);  // the group's slots are free once these complete
+        }
+        mma_commit(&acc_full[b]);
+        bar_arrive(&tab_empty[b]);
+      }
+      // nothing of this block's runs on the tensor cores past this point
+      mma_commit(&done_bar);
+      bar_wait_plain(&done_bar, 0, limit);
+    }
+  } else if (warp < kWarpTma) {
+    // ---- weight builders: voxel m = (x0 + m % 16, z0 + m / 16) = MMA row m;
+    // this thread writes pixels 16 h .. 16 h + 15 of the voxel's weight rows
+    const int m = 32 * (warp & 3) + lane, h = warp >> 2;
+    // byte offset of (voxel m, pixel 8 c) in a weight block: 8 x 16-byte core matrices
+    const unsigned roff = (unsigned)((m >> 3) * 128 + (m & 7) * 16);
+    for (int j = 0, tile = blockIdx.x; tile < ntiles; ++j, tile += gridDim.x) {
+      const int b = j & 1;
+      const TcTile tl = tc_tile(tile, ntx, ntz, NR);
+      const int x = tl.x0 + (m & (kTX - 1)), z = tl.z0 + (m >> 4);
+      const bool inside = x < a.X && z < a.Z;
+      const float xf = voxel_coordf(x, a.X), zf = voxel_coordf(z, a.Z);
+      bar_wait(&tab_full[b], (j >> 1) & 1, limit, a.err, &s_abort);
+      const TcTilt *tab = tilt_tab(b);
+      const TcGroup *gtab = group_tab(b);
+      for (int g = 0; g < ngroups; ++g) {
+        const int G = j * ngroups + g;
+        // the group's weights first (independent tilts: their arithmetic
+        // interleaves), then the wait for its slots
+        unsigned short h0[kG], h1[kG];
+        int pos[kG], blk[kG];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int y = y0 + c + j;
-          if (y < a.Y) a.vol[((size_t)y * a.Z + z) * a.X + x] = __uint_as_float(v[j]) * sc;
+        for (int jj = 0; jj < kG; ++jj) {
+          const int i = min(g * kG + jj, a.T - 1);
+          const TcTilt tt = tab[i];
+          const float4 tc = tconst[i];
+          const float q = detector_coord(__fmul_rn(xf, tc.x), __fmul_rn(zf, tc.y), tc.z);
+          const float r = __fadd_rd(q, kMagic);
+          const int fl = __float_as_int(r) - kMagicBits;
+          const float tw = __fsub_rn(q, __fsub_rn(r, kMagic));
+          const int k = tt.nk > 1 ? slab_index(xf, zf, tc.y, tc.x, a.dscale, a.doffset, a.D)
+                                  : tt.k0;
+          pos[jj] = fl - tt.u0;
+          // the reference skips samples unless 0 <= floor <= N - 2
+          bool valid = inside && fl >= 0 && fl <= a.N - 2;
+          if (valid && (pos[jj] < 0 || pos[jj] > kKW - 2)) {  // excluded by the tile's window
+            valid = false;
+            if (a.err) atomicOr(a.err, 4);
+          }
+          h0[jj] = __half_as_ushort(__float2half_rn(__fmul_rn(__fsub_rn(1.f, tw), tc.w)));
+          h1[jj] = __half_as_ushort(__float2half_rn(__fmul_rn(tw, tc.w)));
+          blk[jj] = valid ? k - tt.k0 : -1;  // the slab block holding the weights
+        }
+        const TcGroup gr = gtab[g];
+        if (gr.w >= 0) bar_wait(&empty[gr.w % kSB], (gr.w / kSB) & 1, limit, a.err, &s_abort);
+#pragma unroll
+        for (int jj = 0; jj < kG; ++jj) {
+          if (g * kG + jj >= a.T) break;
+          const TcTilt tt = tab[g * kG + jj];
+#pragma unroll
+          for (int sl = 0; sl < KMAX; ++sl) {
+            if (sl < tt.nk) {
+              unsigned char *blkp = awts + (size_t)((tt.slot + sl) % R) * kABytes + roff;
+              // this half of the row to zero, then the voxel's two weights
+              *(uint4 *)(blkp + (2 * h) * kAChunk) = make_uint4(0, 0, 0, 0);
+              *(uint4 *)(blkp + (2 * h + 1) * kAChunk) = make_uint4(0, 0, 0, 0);
+              if (blk[jj] == sl) {
+                const int p0 = pos[jj], p1 = pos[jj] + 1;
+                if ((p0 >> 4) == h)
+                  *(unsigned short *)(blkp + (p0 >> 3) * kAChunk + (p0 & 7) * 2) = h0[jj];
+                if ((p1 >> 4) == h)
+                  *(unsigned short *)(blkp + (p1 >> 3) * kAChunk + (p1 & 7) * 2) = h1[jj];
+              }
+            }
+          }
+        }
+        // the tensor cores read the weights through the async proxy
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        bar_arrive(&full[G % kSB]);
+      }
+      bar_arrive(&tab_empty[b]);
+    }
+  } else {
+    // ---- table and store threads: the table of tile j + 1 while tile j is
+    // computed, then tile j's accumulator into the volume
+    const int e = tid - kWarpEpi * 32;
+    const int q = warp & 3, m = 32 * q + lane;
+    const unsigned lane_addr = (unsigned)(32 * q) << 16;
+    const float sc = a.geom[0].scale * pow2f(max(-126, min(127, -e0)));
+    int slot_base = 0;  // the block's running slot count at the next tile's start
+    // the j-th tile's window and slabs per tilt, running slots and group table
+    auto build = [&](int j, int tile) {
+      const int b = j & 1;
+      if (j >= 2) bar_wait(&tab_empty[b], ((j >> 1) - 1) & 1, limit, a.err, &s_abort);
+      TcTilt *tab = tilt_tab(b);
+      TcGroup *gtab = group_tab(b);
+      const TcGroup *prev = group_tab(b ^ 1);
+      const TcTile tl = tc_tile(tile, ntx, ntz, NR);
+      // corners inside the volume (the coordinate and the slab index are
+      // monotone in x and in z)
+      const float cx0 = voxel_coordf(tl.x0, a.X), cx1 = voxel_coordf(min(tl.x0 + kTX, a.X) - 1, a.X);
+      const float cz0 = voxel_coordf(tl.z0, a.Z), cz1 = voxel_coordf(min(tl.z0 + kTZ, a.Z) - 1, a.Z);
+      for (int t = e; t < a.T; t += kEpi) {
+        const float4 tc = tconst[t];
+        const float xc0 = __fmul_rn(cx0, tc.x), xc1 = __fmul_rn(cx1, tc.x);
+        const float zs0 = __fmul_rn(cz0, tc.y), zs1 = __fmul_rn(cz1, tc.y);
+        const float q00 = detector_coord(xc0, zs0, tc.z), q01 = detector_coord(xc0, zs1, tc.z);
+        const float q10 = detector_coord(xc1, zs0, tc.z), q11 = detector_coord(xc1, zs1, tc.z);
+        const int p_lo = floor_int(fminf(fminf(q00, q01), fminf(q10, q11)));
+        int k_lo = 0, k_hi = 0;
+        if (a.D > 1) {
+          const int k00 = slab_index(cx0, cz0, tc.y, tc.x, a.dscale, a.doffset, a.D);
+          const int k01 = slab_index(cx0, cz1, tc.y, tc.x, a.dscale, a.doffset, a.D);
+          const int k10 = slab_index(cx1, cz0, tc.y, tc.x, a.dscale, a.doffset, a.D);
+          const int k11 = slab_index(cx1, cz1, tc.y, tc.x, a.dscale, a.doffset, a.D);
+          k_lo = min(min(k00, k01), min(k10, k11));
+          k_hi = max(max(k00, k01), max(k10, k11));
+        }
+        TcTilt tt;
+        tt.u0 = p_lo & ~7;  // round down to a multiple of 8 (also for negative p_lo)
+        tt.k0 = k_lo;
+        tt.nk = k_hi - k_lo + 1;
+        if (tt.nk > KMAX) {  // excluded by the host's choice of shape
+          tt.nk = KMAX;
+          if (a.err) atomicOr(a.err, 2);
+        }
+        tt.slot = 0;
+        tab[t] = tt;
+      }
+      epi_sync();
+      if (e < 32) {  // running slot counts: a prefix sum of nk over the tilts
+        const int chunk = (a.T + 31) / 32, t0 = e * chunk, t1 = min(a.T, t0 + chunk);
+        int local = 0;
+        for (int t = t0; t < t1; ++t) local += tab[t].nk;
+        int incl = local;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int v = __shfl_up_sync(0xffffffffu, incl, o);
+          if (e >= o) incl += v;
+        }
+        int run = slot_base + incl - local;
+        for (int t = t0; t < t1; ++t) {
+          tab[t].slot = run;
+          run += tab[t].nk;
+        }
+        slot_base += __shfl_sync(0xffffffffu, incl, 31);
+      }
+      epi_sync();
+      for (int g = e; g < ngroups; g += kEpi) {
+        int n = 0;
+        for (int jj = 0; jj < kG && g * kG + jj < a.T; ++jj) n += tab[g * kG + jj].nk;
+        gtab[g].c = tab[g * kG].slot;
+        gtab[g].n = n;
+      }
+      epi_sync();
+      // the group that last used a slot of group g: the one holding running
+      // slot c + n - 1 - R (groups' slots are consecutive).  It lies in this
+      // tile or the one before; for an earlier tile (few slots per tile) the
+      // last group of the tile before that stands in for it (a later group,
+      // so a longer wait, never a shorter one).
+      const int base = gtab[0].c;
+      for (int g = e; g < ngroups; g += kEpi) {
+        const int target = gtab[g].c + gtab[g].n - 1 - R;
+        int w;
+        if (target < 0) w = -1;
+        else if (target >= base) w = j * ngroups + last_group_at(gtab, 0, g - 1, target);
+        else if (target >= prev[0].c) w = (j - 1) * ngroups + last_group_at(prev, 0, ngroups - 1, target);
+        else w = (j - 1) * ngroups - 1;
+        gtab[g].w = w;
+      }
+      bar_arrive(&tab_full[b]);
+    };
+    if (blockIdx.x < ntiles) build(0, blockIdx.x);
+    for (int j = 0, tile = blockIdx.x; tile < ntiles; ++j, tile += gridDim.x) {
+      if (tile + (int)gridDim.x < ntiles) build(j + 1, tile + gridDim.x);
+      const int b = j & 1;
+      const TcTile tl = tc_tile(tile, ntx, ntz, NR);
+      const int x = tl.x0 + (m & (kTX - 1)), z = tl.z0 + (m >> 4);
+      const bool inside = x < a.X && z < a.Z;
+      bar_wait(&acc_full[b], (j >> 1) & 1, limit, a.err, &s_abort);
+      tc_fence_after();
+#pragma unroll 1
+      for (int c = 0; c < NR; c += 32) {
+        unsigned v[32];
+        tmem_ld32(tmem + lane_addr + (unsigned)(b * NR + c), v);
+        if (inside) {
+#pragma unroll
+          for (int i = 0; i < 32; ++i) {
+            const int y = tl.y0 + c + i;
+            if (y < a.Y) a.vol[((size_t)y * a.Z + z) * a.X + x] = __uint_as_float(v[i]) * sc;
+          }
         }
       }
+      tc_fence_before();
+      bar_arrive(&acc_empty[b]);
     }
+  }
+  // after a timeout, the producer waits (boundedly, once more) for the copies
+  // it issued in the last kSB groups, so none lands after the block ends
+  if (s_abort && warp == kWarpTma && lane == 0) {
+    int nt = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) ++nt;
+    const int G1 = nt * ngroups;
+    for (int G = max(0, G1 - kSB); G < G1; ++G) bar_wait_plain(&full[G % kSB], (G / kSB) & 1, limit);
   }
   tc_fence_before();
   __syncthreads();
@@ -576,11 +713,15 @@ static cudaError_t launch_tc(const BpArgs &a, const TcMap &map, cudaStream_t s) 
   using P = TcShape<NR, KMAX, R>;
   auto kern = k_bp_tc<NR, KMAX, R>;
   if (cudaError_t e = ensure_dynamic_smem<k_bp_tc<NR, KMAX, R>>((int)P::kSmem)) return e;
+  int dev = 0, sms = 0;
+  if (cudaError_t e = cudaGetDevice(&dev)) return e;
+  if (cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) return e;
   const int ntx = (a.X + kTX - 1) / kTX, ntz = (a.Z + kTZ - 1) / kTZ;
-  dim3 grid(ntx * ntz, (a.Y + NR - 1) / NR);
+  const int ntiles = ntx * ntz * ((a.Y + NR - 1) / NR);
   CUtensorMap m;
   std::memcpy(&m, map.bytes, sizeof m);
-  kern<<<grid, kThreads, P::kSmem, s>>>(a, m);
+  // one block per SM (the shared memory allows no second), each looping over tiles
+  kern<<<std::min(ntiles, sms), kThreads, P::kSmem, s>>>(a, m);
   return cudaGetLastError();
 }
 
