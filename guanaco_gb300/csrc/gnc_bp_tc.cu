@@ -179,33 +179,29 @@ __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-// Shared-memory descriptor of a weight block: K-major, no swizzle, 8 x 16-byte
-// core matrices; 8-voxel groups 128 bytes apart, 8-pixel groups kAChunk apart.
-__device__ __forceinline__ u64 a_desc(unsigned addr) {
-  u64 d = (u64)((addr & 0x3FFFFu) >> 4);
-  d |= (u64)(kAChunk >> 4) << 16;  // leading offset: next 8 pixels
-  d |= (u64)(128 >> 4) << 32;      // stride offset: next 8 voxels
-  d |= (u64)1 << 46;               // descriptor version
-  return d;                        // layout 0: no swizzle
-}
-// Shared-memory operand descriptor: K-major, 64-byte swizzle, rows of 64
-// bytes in 8-row atoms of 512 bytes (stride between atoms 512 B).
-__device__ __forceinline__ u64 b_desc(unsigned addr) {
-  u64 d = (u64)((addr & 0x3FFFFu) >> 4);
-  d |= (u64)1 << 16;            // leading offset (unused for this layout)
-  d |= (u64)(512 >> 4) << 32;   // stride between 8-row atoms
-  d |= (u64)1 << 46;            // descriptor version
-  d |= (u64)4 << 61;            // 64-byte swizzle
-  return d;
-}
+// Shared-memory matrix descriptors, as two 32-bit halves: bits 0-13 the
+// address / 16, 16-29 the leading offset / 16, 32-45 the stride offset / 16,
+// bit 46 the descriptor version (1), 61-63 the swizzle mode.
+//   A, a weight block: K-major, no swizzle, 8 x 16-byte core matrices;
+//      8-voxel groups 128 bytes apart (stride), 8-pixel groups kAChunk apart
+//      (leading offset).
+//   B, a window: K-major, 64-byte swizzle, rows of 64 bytes in 8-row atoms
+//      of 512 bytes (stride 512 B; the leading offset is unused).
+// The high halves are constants; the low halves are address / 16 plus
+// kALo / kBLo (the address never exceeds 14 bits after the shift).
+constexpr unsigned kALo = (unsigned)(kAChunk >> 4) << 16;
+constexpr unsigned kBLo = 1u << 16;
+constexpr unsigned kAHi = (128u >> 4) | (1u << 14);
+constexpr unsigned kBHi = (512u >> 4) | (1u << 14) | (4u << 29);
+// D[tmem] (+)= A * B^T, FP16 inputs, FP32 accumulator; acc = 0 overwrites.
 // Instruction descriptor: FP16 A and B (K-major), FP32 D, M = 128, N rows
 // (TcShape::kIdesc).
-__device__ __forceinline__ void mma(unsigned d_tmem, u64 adesc, u64 bdesc, unsigned idesc,
+__device__ __forceinline__ void mma(unsigned d_tmem, unsigned a_lo, unsigned b_lo, unsigned idesc,
                                     unsigned acc) {
   asm volatile(
-      "{ .reg .pred p; setp.ne.u32 p, %4, 0; "
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }" ::"r"(d_tmem),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+      "{ .reg .pred p; .reg .b64 ad, bd; setp.ne.u32 p, %6, 0; mov.b64 ad, {%1, %2}; "
+      "mov.b64 bd, {%3, %4}; tcgen05.mma.cta_group::1.kind::f16 [%0], ad, bd, %5, p; }" ::"r"(d_tmem),
+      "r"(a_lo), "r"(kAHi), "r"(b_lo), "r"(kBHi), "r"(idesc), "r"(acc));
 }
 __device__ __forceinline__ void mma_commit(u64 *b) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -366,22 +362,27 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
         bar_wait(&tab_full[b], (j >> 1) & 1, limit, a.err, &s_abort);
         if (j >= 2) bar_wait(&acc_empty[b], ((j >> 1) - 1) & 1, limit, a.err, &s_abort);
         tc_fence_after();
-        const TcTilt *tab = tilt_tab(b);
+        const TcGroup *gtab = group_tab(b);
         const unsigned d = tmem + (unsigned)(b * NR);
+        // descriptors' low halves at slot 0
+        const unsigned a_lo0 = (sa(awts) >> 4) | kALo;
+        const unsigned b_lo0 = (sa(bwin) >> 4) | kBLo;
+        unsigned acc = 0;  // the tile's first MMA overwrites the accumulator
         for (int g = 0; g < ngroups; ++g) {
           const int G = j * ngroups + g;
           bar_wait(&full[G % kSB], (G / kSB) & 1, limit, a.err, &s_abort);
           tc_fence_after();
-          for (int jj = 0; jj < kG && g * kG + jj < a.T; ++jj) {
-            const TcTilt tt = tab[g * kG + jj];
-            for (int sl = 0; sl < tt.nk; ++sl) {
-              const int slot = (tt.slot + sl) % R;
-              const unsigned ab = sa(awts + (size_t)slot * kABytes);
-              const unsigned bb = sa(bwin + (size_t)slot * P::kBBytes);
-              for (int kk = 0; kk < 2; ++kk)
-                mma(d, a_desc(ab + kk * 2 * kAChunk), b_desc(bb + kk * 32), P::kIdesc,
-                    (g | jj | sl | kk) != 0 ? 1u : 0u);
-            }
+          // a group's slots are consecutive: running slots c .. c + n - 1,
+          // tilt by tilt and slab by slab
+          const TcGroup gr = gtab[g];
+          int slot = gr.c % R;
+          for (int i = 0; i < gr.n; ++i) {
+            const unsigned a_lo = a_lo0 + (unsigned)slot * (kABytes >> 4);
+            const unsigned b_lo = b_lo0 + (unsigned)slot * (P::kBBytes >> 4);
+            mma(d, a_lo, b_lo, P::kIdesc, acc);  // pixels 0-15, then 16-31
+            mma(d, a_lo + (2 * kAChunk >> 4), b_lo + (32 >> 4), P::kIdesc, 1);
+            acc = 1;
+            slot = slot + 1 == R ? 0 : slot + 1;
           }
           mma_commit(&empty[G % kSB]);  // the group's slots are free once these complete
         }
