@@ -13,10 +13,10 @@
 //   * the 32-pixel window [u0, u0 + 32) of the NR rows (u0 a multiple of 8),
 //     brought by one TMA load, 64-byte swizzled (the MMA's B operand);
 //   * the 128 x 32 FP16 weights of the slab (the A operand, K-major, no
-//     swizzle), written by 256 builder threads -- two per voxel, one per half
-//     of the window -- that compute the voxel's detector coordinate, floor,
-//     weight and slab with the reference's float operations, zero their half
-//     row and store the voxel's two weights when its slab is the slot's;
+//     swizzle), written by 256 builder threads -- two per voxel, one per tilt
+//     of a group -- that compute the voxel's detector coordinate, floor,
+//     weight and slab with the reference's float operations, zero the row
+//     and store the voxel's two weights when its slab is the slot's;
 // and one thread issues two tcgen05.mma per slot (M 128 voxels, N NR rows,
 // K 16 pixels each) accumulating into the 128 x NR FP32 tile in tensor
 // memory.  Weights carry the tilt's factor 2^(E0 - e(t)) (E0 the smallest
@@ -48,11 +48,15 @@
 // in tensor memory (tcgen05.st of all 32 words per voxel) 2.41 ms; weights in
 // shared memory, two 16-byte zero stores and two 2-byte weight stores per
 // thread and slot, 2.17 ms; persistent with the table and store overlapped
-// 1.69 ms.  Clock stamps of the non-persistent form put 39 % of a block's time
+// 1.69 ms; the MMA issuer on 32-bit descriptor halves 1.62 ms.  Timing-only
+// variants of the last (wrong volumes, every wait kept): without the window
+// loads and the weight stores 1.21 ms, without the builders' arithmetic as
+// well 1.05 ms (1.34 PFLOP/s, 71 % of the measured cuBLAS peak).  Clock stamps of the non-persistent form put 39 % of a block's time
 // outside the group loop (table 8 %, pipeline fill 7 %, drain 5 %, volume
-// stores 19 %), and inside it a group period of ~1400 cycles against ~990 of
-// MMA issue: shared memory bandwidth (window writes, operand reads, weight
-// stores) is the loop's bound.  Prefetching the windows of later tilts into
+// stores 19 %).  Inside it, per slab slot, the window's TMA write (NR x 64 B),
+// the MMA's operand reads (window and weights) and the weight stores move
+// about 48 KB of shared memory against 32 KB per 256 MMA cycles at 128 B per
+// cycle: shared memory bandwidth is the loop's bound.  Prefetching the windows of later tilts into
 // L2 made the kernel 25 % slower (the prefetches compete with the loads).
 // Every wait is bounded and records a timeout in the plan's error word; after
 // one timeout the block's remaining waits return at once.
@@ -71,7 +75,7 @@ namespace {
 constexpr int kTX = 16, kTZ = 8;  // voxel tile (x, z): 128 voxels = M
 constexpr int kKW = 32;           // window pixels (two K = 16 steps)
 constexpr int kG = 2;             // tilts per group: one barrier round trip per group
-constexpr int kQ = 2;             // builder threads per voxel (window halves)
+constexpr int kQ = 2;             // builder threads per voxel (one per tilt of a group)
 constexpr int kBuilders = 128 * kQ;       // warps 0-7
 constexpr int kEpi = 128;                 // table and store threads: warps 10-13
 constexpr int kThreads = kBuilders + 64 + kEpi;
@@ -395,7 +399,9 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
     }
   } else if (warp < kWarpTma) {
     // ---- weight builders: voxel m = (x0 + m % 16, z0 + m / 16) = MMA row m;
-    // this thread writes pixels 16 h .. 16 h + 15 of the voxel's weight rows
+    // warps w and w + 4 write the weight rows of voxels 32 (w % 4) .. for the
+    // group's first and second tilt
+    static_assert(kQ == kG, "one builder thread per voxel and tilt of a group");
     const int m = 32 * (warp & 3) + lane, h = warp >> 2;
     // byte offset of (voxel m, pixel 8 c) in a weight block: 8 x 16-byte core matrices
     const unsigned roff = (unsigned)((m >> 3) * 128 + (m & 7) * 16);
@@ -410,14 +416,13 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
       const TcGroup *gtab = group_tab(b);
       for (int g = 0; g < ngroups; ++g) {
         const int G = j * ngroups + g;
-        // the group's weights first (independent tilts: their arithmetic
-        // interleaves), then the wait for its slots
-        unsigned short h0[kG], h1[kG];
-        int pos[kG], blk[kG];
-#pragma unroll
-        for (int jj = 0; jj < kG; ++jj) {
-          const int i = min(g * kG + jj, a.T - 1);
-          const TcTilt tt = tab[i];
+        // the weights first, then the wait for the group's slots
+        const int i = g * kG + h;
+        const bool has = i < a.T;  // the last group of an odd tilt count has one tilt
+        const TcTilt tt = tab[min(i, a.T - 1)];
+        int pos = 0, blk = -1;
+        unsigned short h0 = 0, h1 = 0;
+        if (has) {
           const float4 tc = tconst[i];
           const float q = detector_coord(__fmul_rn(xf, tc.x), __fmul_rn(zf, tc.y), tc.z);
           const float r = __fadd_rd(q, kMagic);
@@ -425,36 +430,31 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
           const float tw = __fsub_rn(q, __fsub_rn(r, kMagic));
           const int k = tt.nk > 1 ? slab_index(xf, zf, tc.y, tc.x, a.dscale, a.doffset, a.D)
                                   : tt.k0;
-          pos[jj] = fl - tt.u0;
+          pos = fl - tt.u0;
           // the reference skips samples unless 0 <= floor <= N - 2
           bool valid = inside && fl >= 0 && fl <= a.N - 2;
-          if (valid && (pos[jj] < 0 || pos[jj] > kKW - 2)) {  // excluded by the tile's window
+          if (valid && (pos < 0 || pos > kKW - 2)) {  // excluded by the tile's window
             valid = false;
             if (a.err) atomicOr(a.err, 4);
           }
-          h0[jj] = __half_as_ushort(__float2half_rn(__fmul_rn(__fsub_rn(1.f, tw), tc.w)));
-          h1[jj] = __half_as_ushort(__float2half_rn(__fmul_rn(tw, tc.w)));
-          blk[jj] = valid ? k - tt.k0 : -1;  // the slab block holding the weights
+          h0 = __half_as_ushort(__float2half_rn(__fmul_rn(__fsub_rn(1.f, tw), tc.w)));
+          h1 = __half_as_ushort(__float2half_rn(__fmul_rn(tw, tc.w)));
+          blk = valid ? k - tt.k0 : -1;  // the slab block holding the weights
         }
         const TcGroup gr = gtab[g];
         if (gr.w >= 0) bar_wait(&empty[gr.w % kSB], (gr.w / kSB) & 1, limit, a.err, &s_abort);
-#pragma unroll
-        for (int jj = 0; jj < kG; ++jj) {
-          if (g * kG + jj >= a.T) break;
-          const TcTilt tt = tab[g * kG + jj];
+        if (has) {
 #pragma unroll
           for (int sl = 0; sl < KMAX; ++sl) {
             if (sl < tt.nk) {
               unsigned char *blkp = awts + (size_t)((tt.slot + sl) % R) * kABytes + roff;
-              // this half of the row to zero, then the voxel's two weights
-              *(uint4 *)(blkp + (2 * h) * kAChunk) = make_uint4(0, 0, 0, 0);
-              *(uint4 *)(blkp + (2 * h + 1) * kAChunk) = make_uint4(0, 0, 0, 0);
-              if (blk[jj] == sl) {
-                const int p0 = pos[jj], p1 = pos[jj] + 1;
-                if ((p0 >> 4) == h)
-                  *(unsigned short *)(blkp + (p0 >> 3) * kAChunk + (p0 & 7) * 2) = h0[jj];
-                if ((p1 >> 4) == h)
-                  *(unsigned short *)(blkp + (p1 >> 3) * kAChunk + (p1 & 7) * 2) = h1[jj];
+              // the row to zero, then the voxel's two weights
+#pragma unroll
+              for (int c = 0; c < kKW / 8; ++c)
+                *(uint4 *)(blkp + c * kAChunk) = make_uint4(0, 0, 0, 0);
+              if (blk == sl) {
+                *(unsigned short *)(blkp + (pos >> 3) * kAChunk + (pos & 7) * 2) = h0;
+                *(unsigned short *)(blkp + ((pos + 1) >> 3) * kAChunk + ((pos + 1) & 7) * 2) = h1;
               }
             }
           }
