@@ -444,9 +444,11 @@ def serving_desc(r):
 
 def drive_stream(srv, stream, descs, inputs, pools, t_base):
     """Submits each request at its arrival time (server clock t_base + arrival);
-    returns per-request (latency s, voxel-tilts, info).  A request whose output
-    pool is empty waits for the oldest one of its size (client back-pressure);
-    its latency still counts from the scheduled arrival."""
+    returns per-request (latency s, voxel-tilts, info).  Finished requests are
+    collected in the order they finish (one wait_any call each, so the client's
+    cost per request does not grow with the backlog).  A request whose output
+    pool is empty waits until a request of its size finishes (client
+    back-pressure); its latency still counts from the scheduled arrival."""
     outstanding = {}
     done = []
 
@@ -455,28 +457,28 @@ def drive_stream(srv, stream, descs, inputs, pools, t_base):
         pools[r["size"]].append(buf)
         done.append((info["t_done"] - (t_base + r["arrival"]), descs[r["id"]].voxel_tilts, info))
 
-    def reap():
-        for rid in list(outstanding):
-            info = srv.wait(rid, timeout=0.0)
-            if info is not None:
-                finish(rid, info)
+    def collect(timeout):
+        got = srv.wait_any(timeout)
+        if got is not None:
+            finish(*got)
+        return got is not None
 
     for r in stream:
         target = t_base + r["arrival"]
         while True:
-            reap()
+            while collect(0.0):
+                pass
             now = srv.now()
             if now >= target:
                 break
             time.sleep(min(target - now, 2e-4))
         while not pools[r["size"]]:
-            rid = min((k for k, v in outstanding.items() if v[0]["size"] == r["size"]))
-            finish(rid, srv.wait(rid))
+            collect(None)
         buf = pools[r["size"]].pop()
         rid = srv.submit(descs[r["id"]], inputs[(r["size"], r["tilts"])], buf)
         outstanding[rid] = (r, buf)
-    for rid in list(outstanding):
-        finish(rid, srv.wait(rid))
+    while outstanding:
+        collect(None)
     return done
 
 

@@ -153,6 +153,8 @@ SIGNATURES = {
                                   ctypes.POINTER(ctypes.c_uint64)]),
     "gnc_server_wait": (c_int, [c_void, ctypes.c_uint64, c_double,
                                 ctypes.POINTER(GncRequestInfo)]),
+    "gnc_server_wait_any": (c_int, [c_void, c_double, ctypes.POINTER(ctypes.c_uint64),
+                                    ctypes.POINTER(GncRequestInfo)]),
     "gnc_server_now": (c_double, [c_void]),
     "gnc_server_get_stats": (c_int, [c_void, ctypes.POINTER(GncServerStats)]),
 }

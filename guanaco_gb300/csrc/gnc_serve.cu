@@ -101,6 +101,9 @@ struct gnc_server {
   std::vector<Slot> slots;
   std::deque<Request *> queue;
   std::unordered_map<uint64_t, std::unique_ptr<Request>> reqs;
+  // ids of finished requests in the order they finished, for
+  // gnc_server_wait_any (ids already collected by gnc_server_wait are skipped)
+  std::deque<uint64_t> finished;
   std::vector<std::unique_ptr<Cached>> cache;
   std::mutex mu;
   std::condition_variable cv_sched, cv_done, cv_build;
@@ -197,10 +200,27 @@ size_t idle_bytes(gnc_server *S) {
   return b;
 }
 
-// Under the lock: finish the requests whose slots reported back.
+// Under the lock: r has finished; gnc_server_wait_any reports it in this order.
+void mark_done(gnc_server *S, Request *r) {
+  r->done = true;
+  S->finished.push_back(r->id);
+  if (S->finished.size() > 2 * S->reqs.size() + 64) {  // drop ids collected by id
+    std::deque<uint64_t> keep;
+    for (uint64_t id : S->finished)
+      if (S->reqs.count(id)) keep.push_back(id);
+    S->finished.swap(keep);
+  }
+}
+
+// Under the lock: finish the requests whose slots reported back, in the
+// order they finished.
 void reap(gnc_server *S) {
-  for (Slot &sl : S->slots) {
-    if (!sl.req || !sl.finished) continue;
+  std::vector<Slot *> fin;
+  for (Slot &sl : S->slots)
+    if (sl.req && sl.finished) fin.push_back(&sl);
+  std::sort(fin.begin(), fin.end(), [](const Slot *a, const Slot *b) { return a->t_done < b->t_done; });
+  for (Slot *slp : fin) {
+    Slot &sl = *slp;
     Request *r = sl.req;
     r->t_done = sl.t_done;
     r->device_error = *sl.h_err != 0;
@@ -208,7 +228,7 @@ void reap(gnc_server *S) {
       r->status = GNC_ERR_CUDA;
       r->error = "a bounded wait in a kernel gave up (device error word set)";
     }
-    r->done = true;
+    mark_done(S, r);
     sl.plan->busy = false;
     sl.plan->last_use = ++S->tick;
     sl.req = nullptr;
@@ -226,8 +246,8 @@ void reap(gnc_server *S) {
 void fail(gnc_server *S, Request *r, int status, const std::string &msg) {
   r->status = status;
   r->error = msg;
-  r->done = true;
   r->t_done = S->now();
+  mark_done(S, r);
   S->st.failed++;
 }
 
@@ -455,6 +475,26 @@ void run(gnc_server *S) {
 
 using gnc::set_error;
 
+namespace {
+// Under the lock: a finished request's outcome into info, then forgotten.
+int collect(gnc_server *S, std::unordered_map<uint64_t, std::unique_ptr<Request>>::iterator it,
+            gnc_request_info *info) {
+  Request *r = it->second.get();
+  if (info) {
+    info->status = r->status;
+    info->graph = r->graph;
+    info->device_error = r->device_error;
+    info->t_submit = r->t_submit;
+    info->t_start = r->t_start;
+    info->t_done = r->t_done;
+  }
+  const int status = r->status;
+  if (status != GNC_OK) gnc::set_error(r->error);
+  S->reqs.erase(it);
+  return status;
+}
+}  // namespace
+
 extern "C" {
 
 int gnc_server_create(size_t budget_bytes, int slots, gnc_server **server) {
@@ -614,18 +654,29 @@ int gnc_server_wait(gnc_server *S, uint64_t id, double timeout_s, gnc_request_in
   else
     S->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), pred);
   if (!r->done) return GNC_ERR_PENDING;
-  if (info) {
-    info->status = r->status;
-    info->graph = r->graph;
-    info->device_error = r->device_error;
-    info->t_submit = r->t_submit;
-    info->t_start = r->t_start;
-    info->t_done = r->t_done;
+  return collect(S, it, info);
+}
+
+int gnc_server_wait_any(gnc_server *S, double timeout_s, uint64_t *id, gnc_request_info *info) {
+  if (!S || !id) {
+    set_error("gnc_server_wait_any: ASSERT (server != nullptr && id != nullptr) failed");
+    return GNC_ERR_INVALID_ARGUMENT;
   }
-  const int status = r->status;
-  if (status != GNC_OK) set_error(r->error);
-  S->reqs.erase(it);
-  return status;
+  std::unique_lock<std::mutex> lk(S->mu);
+  auto ready = [S] {
+    while (!S->finished.empty() && !S->reqs.count(S->finished.front())) S->finished.pop_front();
+    return !S->finished.empty();
+  };
+  // nothing submitted and uncollected: nothing to wait for
+  auto pred = [S, &ready] { return ready() || S->reqs.empty(); };
+  if (timeout_s < 0)
+    S->cv_done.wait(lk, pred);
+  else
+    S->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), pred);
+  if (!ready()) return GNC_ERR_PENDING;
+  *id = S->finished.front();
+  S->finished.pop_front();
+  return collect(S, S->reqs.find(*id), info);
 }
 
 double gnc_server_now(const gnc_server *S) { return S ? S->now() : 0.0; }

@@ -78,7 +78,27 @@ class Server:
                                        ctypes.byref(info))
         if st == _lib.GNC_ERR_PENDING:
             return None
-        self._live.pop(int(rid), None)
+        return self._collected(int(rid), st, info)
+
+    def wait_any(self, timeout=None):
+        """Wait for whichever request finishes next (in the order requests
+        finish); returns ``(id, info)``, or None if none finished within the
+        timeout or none is outstanding.  A failed request raises GncError with
+        ``info`` and ``rid`` attached."""
+        info = _lib.GncRequestInfo()
+        rid = ctypes.c_uint64()
+        st = self._lib.gnc_server_wait_any(self._h, -1.0 if timeout is None else timeout,
+                                           ctypes.byref(rid), ctypes.byref(info))
+        if st == _lib.GNC_ERR_PENDING:
+            return None
+        try:
+            return rid.value, self._collected(rid.value, st, info)
+        except _lib.GncError as e:
+            e.rid = rid.value
+            raise
+
+    def _collected(self, rid, st, info):
+        self._live.pop(rid, None)
         out = {"status": info.status, "graph": bool(info.graph),
                "device_error": bool(info.device_error), "t_submit": info.t_submit,
                "t_start": info.t_start, "t_done": info.t_done}

@@ -335,6 +335,14 @@ GNC_API int gnc_server_submit(gnc_server *server, const gnc_fbp_desc *desc, cons
  * (may be NULL); a finished request is forgotten after this call. */
 GNC_API int gnc_server_wait(gnc_server *server, uint64_t id, double timeout_s,
                             gnc_request_info *info);
+/* Waits up to timeout_s seconds (< 0: forever) for any request that has
+ * finished and not been collected (by this call or gnc_server_wait), in the
+ * order requests finish; sets *id and returns as gnc_server_wait does for it.
+ * Returns GNC_ERR_PENDING if none finished in time, at once if no request is
+ * outstanding.  A client serving a stream collects each request with one call
+ * instead of polling every outstanding id. */
+GNC_API int gnc_server_wait_any(gnc_server *server, double timeout_s, uint64_t *id,
+                                gnc_request_info *info);
 /* Seconds since the server was created (the clock of gnc_request_info). */
 GNC_API double gnc_server_now(const gnc_server *server);
 GNC_API int gnc_server_get_stats(gnc_server *server, gnc_server_stats *stats);

@@ -142,3 +142,37 @@ def test_oversize_and_invalid_requests_fail_at_submit(G):
             srv.submit(d_bad, np.zeros(d_bad.input_shape, np.float32),
                        np.empty(d_bad.volume_shape, np.float32))
         assert e.value.status == _lib.GNC_ERR_UNSUPPORTED
+
+
+def test_wait_any_reports_each_request_once_in_finishing_order(G):
+    from guanaco_gb300 import serve
+
+    shapes = [(64, 11, 3, "f32"), (128, 21, 5, "f16"), (96, 9, 1, "f32"), (64, 11, 3, "f32"),
+              (128, 13, 3, "f16t"), (96, 9, 1, "f32")]
+    reqs = []
+    for i, (n, T, D, st) in enumerate(shapes):
+        args, kw, proj = _request(G, n, T, D, st, seed=200 + i)
+        reqs.append((G.FbpDesc(*args, **kw), proj, _alone(G, args, kw, proj)))
+    with serve.Server(budget_bytes=8 << 30, slots=3) as srv:
+        assert srv.wait_any(0.0) is None  # nothing outstanding: no wait
+        outs, ids = {}, []
+        for d, proj, want in reqs:
+            out = np.full(d.volume_shape, np.nan, np.float32)
+            rid = srv.submit(d, proj, out)
+            ids.append(rid)
+            outs[rid] = (out, want)
+        # one collected by id first; wait_any then reports each other request once
+        first = srv.wait(ids[2])
+        seen = []
+        while True:
+            got = srv.wait_any(None)
+            if got is None:
+                break
+            seen.append(got)
+        assert srv.wait_any(None) is None  # all collected: returns at once
+    assert sorted(r for r, _ in seen) == sorted(ids[:2] + ids[3:])
+    done_times = [info["t_done"] for _, info in seen]
+    assert done_times == sorted(done_times)  # in the order the requests finished
+    assert first["status"] == 0
+    for rid, (out, want) in outs.items():
+        np.testing.assert_array_equal(out, want)
