@@ -47,7 +47,7 @@ WORKLOAD_NAME = ("3D CTF ndf=10: 61 tilts +-60 deg, 1024x1024 projections at 1.0
 # DRAM bytes (read + written) of one backprojection launch on this workload,
 # from an ncu capture whose summary (command included) is committed beside the
 # other profiles; the line names the file it came from.
-TRAFFIC_CAPTURE = os.path.join("profiles", "k_bp_fast_dram_3dctf_ndf10.txt")
+TRAFFIC_CAPTURE = os.path.join("profiles", "bp_dram_3dctf_ndf10.md")
 
 
 def bp_traffic(form):
@@ -62,6 +62,51 @@ def bp_traffic(form):
     except OSError:
         pass
     return None, f"no capture of the {form} backprojector in {TRAFFIC_CAPTURE}"
+
+
+def tc_mma_flops():
+    """FLOPs of the tensor-core backprojector's MMAs on the workload: per row
+    band (256 rows when every 16 x 8 voxel tile reaches at most two slabs per
+    tilt, else 128), tile and tilt, the slabs between the lowest and highest
+    slab of the tile's four corner voxels inside the volume (the kernel's table
+    rule, evaluated here in float32), each two MMAs of M 128 x N rows x K 16.
+    (rows, flops)."""
+    T, H, W, Z = WL["T"], WL["H"], WL["W"], WL["Z"]
+    c, mn, mx, step, nd = slab_setup()
+    df = WL["defocus"]
+    mind, maxd = np.float32(mn - df), np.float32(mx - df)
+    px = np.float32(WL["pixel_size"])
+    ds = np.float32(nd * px / (maxd - mind)) if nd > 1 else np.float32(0)
+    doff = np.float32(-ds * np.float32(mind / px))
+    th = angles_rad()
+    co, si = np.cos(th).astype(np.float32), np.sin(th).astype(np.float32)
+    d = co * co + si * si
+    cos_a, sin_a = co / d, si / d
+
+    def coord(i, n):
+        return (i.astype(np.float64) - 0.5 * n + 0.5).astype(np.float32)
+
+    x0 = np.arange(0, W, 16)
+    z0 = np.arange(0, Z, 8)
+    cx = [coord(x0, W), coord(np.minimum(x0 + 16, W) - 1, W)]
+    cz = [coord(z0, Z), coord(np.minimum(z0 + 8, Z) - 1, Z)]
+    per_tilt = []
+    for t in range(T):
+        ks = []
+        for x in cx:
+            for z in cz:
+                h = ((-x[:, None] * sin_a[t]).astype(np.float32)
+                     - (z[None, :] * cos_a[t]).astype(np.float32))
+                dd = (h * ds).astype(np.float32) + doff
+                fl = np.floor(dd)
+                k = fl + ((dd - fl) >= 0.5)
+                ks.append(np.clip(k, 0, nd - 1))
+        per_tilt.append(np.max(ks, 0) - np.min(ks, 0) + 1 if nd > 1
+                        else np.ones((len(x0), len(z0))))
+    nk = np.stack(per_tilt)
+    rows = 256 if nk.max() <= 2 else 128
+    slots = float(nk.sum()) * ((H + rows - 1) // rows)
+    return rows, slots * 2 * (2 * 128 * rows * 16)
 
 
 def angles_rad():
@@ -318,6 +363,31 @@ def run_ours(args, rank, world, dist):
     live = p32.live_slabs(stream)
     live_pairs = int((live[:, 1] - live[:, 0] + 1).sum())
     stage_flops = fft_flops(live_pairs if WL["ctf"] else None)
+    # the F16T form's backprojector against the tensor peak: the FLOPs its MMAs
+    # execute (weights of two pixels per voxel padded to 32-pixel windows, so
+    # most of them multiply zeros) over its event time, and its DRAM traffic
+    tc_roofline = None
+    if plans["f16t"].backprojector == 16 and WL["ctf"]:
+        tc_rows, tc_flops = tc_mma_flops()
+        tc_ms = res["f16t"][1]
+        bf16_peak = peaks.get("bf16_tflops", 1900.0)
+        tc_traffic, tc_src = bp_traffic("f16t")
+        tc_roofline = {
+            "kernel": f"k_bp_tc<{tc_rows},...> (tensor-core backprojection)",
+            "bound": "tensor",
+            "achieved": round(tc_flops / (tc_ms * 1e-3) / 1e12, 1),
+            "peak": bf16_peak,
+            "peak_source": ("measured (cuBLAS bf16 burst)" if "bf16_tflops" in peaks
+                            else "fallback"),
+            "unit": "TFLOP/s",
+            "frac": round(tc_flops / (tc_ms * 1e-3) / 1e12 / bf16_peak, 4),
+            "mma_flops_per_launch": tc_flops,
+            "flops_source": "MMA slots counted on the host from the tiles' corner slabs",
+            "traffic": tc_traffic if args.case == "3dctf" else None,
+            "traffic_source": tc_src if args.case == "3dctf" else "no capture for this case",
+            "hbm_frac": (round(tc_traffic / (tc_ms * 1e-3) / 1e9 / hbm_peak, 4)
+                         if tc_traffic and args.case == "3dctf" else None),
+        }
     line = {
         "metric": METRIC,
         "value": round(value32, 2),
@@ -351,7 +421,8 @@ def run_ours(args, rank, world, dist):
                      "bp_ms": round(res["f16t"][1], 4),
                      "speedup_vs_f32": round(value16t / value32, 3),
                      "staging": ("FP16 rows, one power-of-two scale per tilt, tensor-core "
-                                 "backprojection (tcgen05, FP32 accumulation)")},
+                                 "backprojection (tcgen05, FP32 accumulation)"),
+                     "roofline": tc_roofline},
         },
         "e2e": {
             "value": round(e2e_value, 2), "unit": UNIT,
