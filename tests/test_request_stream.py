@@ -19,7 +19,9 @@ def test_stream_ranges():
     assert {r["size"] for r in s} == {128, 256, 384, 512}
     assert {r["tilts"] for r in s} == {31, 41, 61}
     assert {r["ndf"] for r in s} == set(range(1, 11))
-    assert {r["staging"] for r in s} == {"f16", "f32"}
+    assert {r["staging"] for r in s} == {"f16t", "f32"}
+    assert {r["staging"] for r in request_stream(200, 1000.0, seed=1, f16_form="f16")} == {
+        "f16", "f32"}
     assert all(10000.0 <= r["defocus"] <= 50000.0 for r in s)
     assert all(r["thickness"] == r["size"] // 2 for r in s)
     # Poisson arrivals: mean gap 1/rate, coefficient of variation about 1
