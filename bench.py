@@ -293,9 +293,10 @@ def run_ours(args, rank, world, dist):
 
     clocks = ClockSampler(dev.index)
     clocks.start()
-    res = {}
+    res, backprojector = {}, {}
     for form in (("f16", "f16t", "f32") if large else ("f32", "f16", "f16t")):
         res[form] = timed(form)
+        backprojector[form] = plans[form].backprojector
         if large and form != "f32":  # one plan at a time in HBM at this size
             plans.pop(form).close()
             vols.pop(form)
@@ -367,7 +368,7 @@ def run_ours(args, rank, world, dist):
     # execute (weights of two pixels per voxel padded to 32-pixel windows, so
     # most of them multiply zeros) over its event time, and its DRAM traffic
     tc_roofline = None
-    if plans["f16t"].backprojector == 16 and WL["ctf"]:
+    if backprojector["f16t"] == 16 and WL["ctf"]:
         tc_rows, tc_flops = tc_mma_flops()
         tc_ms = res["f16t"][1]
         bf16_peak = peaks.get("bf16_tflops", 1900.0)
