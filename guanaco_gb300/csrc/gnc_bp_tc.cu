@@ -33,30 +33,32 @@
 // accumulator j % 2 of tensor memory (2 x NR columns) and reads table buffer
 // j % 2, so the next tile's table is built and the last tile's accumulator is
 // stored while the current tile runs.  Warp roles (448 threads): warps 0-7
-// build weights (warps w and w + 4 the two window halves of voxels 32 (w % 4)
-// ..), warp 8 issues the TMA loads, warp 9 owns the tensor memory and issues
-// the MMAs, warps 10-13 build each tile's tilt and group tables and store the
-// accumulators.  Tilts go in groups of kG, each with a "full" mbarrier (the
-// builders and the producer arrive, the windows' bytes complete it) and an
-// "empty" one (the MMAs' commit); group numbers and slot counts run on across
-// a block's tiles.  A group's slots are consecutive in the ring, so before
-// filling them the producer and the builders wait for the one earlier group
-// that last used the newest of them, found when the table is built.  The
-// builders compute a group's weights before that wait.
+// build weights (warps w and w + 4 the first and second tilt of a group for
+// voxels 32 (w % 4) ..), warp 8 issues the TMA loads (one lane per copy of a
+// group), warp 9 owns the tensor memory and issues the MMAs, warps 10-13
+// build each tile's tilt and group tables and store the accumulators.  Tilts
+// go in groups of kG, each with a "full" mbarrier (the builders and the
+// producer arrive, the windows' bytes complete it) and an "empty" one (the
+// MMAs' commit); group numbers and slot counts run on across a block's tiles.
+// A group's slots are consecutive in the ring, so before filling them the
+// producer and the builders wait for the one earlier group that last used the
+// newest of them, found when the table is built.  The builders compute a
+// group's weights before that wait.
 //
 // Measured on the 61-tilt 1024 x 1024 x 300 ten-slab series (GB300): weights
 // in tensor memory (tcgen05.st of all 32 words per voxel) 2.41 ms; weights in
 // shared memory, two 16-byte zero stores and two 2-byte weight stores per
 // thread and slot, 2.17 ms; persistent with the table and store overlapped
-// 1.69 ms; the MMA issuer on 32-bit descriptor halves 1.62 ms.  Timing-only
-// variants of the last (wrong volumes, every wait kept): without the window
-// loads and the weight stores 1.21 ms, without the builders' arithmetic as
-// well 1.05 ms (1.34 PFLOP/s, 71 % of the measured cuBLAS peak).  Clock stamps of the non-persistent form put 39 % of a block's time
-// outside the group loop (table 8 %, pipeline fill 7 %, drain 5 %, volume
-// stores 19 %).  Inside it, per slab slot, the window's TMA write (NR x 64 B),
-// the MMA's operand reads (window and weights) and the weight stores move
-// about 48 KB of shared memory against 32 KB per 256 MMA cycles at 128 B per
-// cycle: shared memory bandwidth is the loop's bound.  Prefetching the windows of later tilts into
+// 1.69 ms; the MMA issuer on 32-bit descriptor halves 1.62 ms; copies issued
+// one lane per copy 1.60 ms.  What bounds the group loop is the window copies:
+// without them (a timing-only variant, wrong volumes, every wait kept) it
+// takes 1.10 ms, without the weight stores 1.61 ms, and clock stamps show the
+// MMA thread waiting some 700 of a group's 1400 cycles for windows; a 256-row
+// box of 64-byte rows keeps the copy engine busy about 300 cycles, one row per
+// cycle.  Halving the bytes per voxel (16 x 16 tiles, two MMA groups sharing
+// 128-row windows) and a deeper window ring (copies four groups ahead) did not
+// change the time, so the engine's rate for narrow rows, not the bytes or the
+// latency, is the bound.  Prefetching the windows of later tilts into
 // L2 made the kernel 25 % slower (the prefetches compete with the loads).
 // Every wait is bounded and records a timeout in the plan's error word; after
 // one timeout the block's remaining waits return at once.
@@ -328,35 +330,42 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
   const unsigned tmem = tmem_base;
 
   if (warp == kWarpTma) {
-    // ---- TMA producer: each slab's window into its slot
-    if (lane == 0) {
-      for (int j = 0, tile = blockIdx.x; tile < ntiles; ++j, tile += gridDim.x) {
-        const int b = j & 1;
-        bar_wait(&tab_full[b], (j >> 1) & 1, limit, a.err, &s_abort);
-        const TcTilt *tab = tilt_tab(b);
-        const TcGroup *gtab = group_tab(b);
-        const int yrow = a.y_begin + tc_tile(tile, ntx, ntz, NR).y0;
-        for (int g = 0; g < ngroups; ++g) {
-          const int G = j * ngroups + g;
-          const TcGroup gr = gtab[g];
+    // ---- TMA producer: each slab's window into its slot.  Issuing one copy
+    // takes a thread some 300 cycles, so lane l issues the group's l-th copy
+    // (after lane 0 has armed the group's barrier for all of them).
+    for (int j = 0, tile = blockIdx.x; tile < ntiles; ++j, tile += gridDim.x) {
+      const int b = j & 1;
+      if (lane == 0) bar_wait(&tab_full[b], (j >> 1) & 1, limit, a.err, &s_abort);
+      __syncwarp();
+      const TcTilt *tab = tilt_tab(b);
+      const TcGroup *gtab = group_tab(b);
+      const int yrow = a.y_begin + tc_tile(tile, ntx, ntz, NR).y0;
+      for (int g = 0; g < ngroups; ++g) {
+        const int G = j * ngroups + g;
+        const TcGroup gr = gtab[g];
+        if (lane == 0) {
           if (gr.w >= 0) bar_wait(&empty[gr.w % kSB], (gr.w / kSB) & 1, limit, a.err, &s_abort);
           bar_expect_tx(&full[G % kSB], (unsigned)(gr.n * P::kBBytes));
-          for (int jj = 0; jj < kG && g * kG + jj < a.T; ++jj) {
-            const int i = g * kG + jj;
-            const TcTilt tt = tab[i];
-            for (int sl = 0; sl < tt.nk; ++sl) {
-              const int slot = (tt.slot + sl) % R;
-              asm volatile(
-                  "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes "
-                  "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(sa(bwin + (size_t)slot * P::kBBytes)),
-                  "l"(&map), "r"(tt.u0), "r"(yrow), "r"((tt.k0 + sl) * a.T + i),
-                  "r"(sa(&full[G % kSB]))
-                  : "memory");
-            }
-          }
         }
-        bar_arrive(&tab_empty[b]);
+        __syncwarp();
+        if (lane < gr.n) {
+          // copy `lane` of the group: the tilts' slabs in order
+          const int i0 = g * kG;
+          const int n0 = tab[i0].nk;
+          const int i = lane < n0 ? i0 : i0 + 1;
+          const int sl = lane < n0 ? lane : lane - n0;
+          const TcTilt tt = tab[i];
+          const int slot = (gr.c + lane) % R;
+          asm volatile(
+              "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes "
+              "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(sa(bwin + (size_t)slot * P::kBBytes)),
+              "l"(&map), "r"(tt.u0), "r"(yrow), "r"((tt.k0 + sl) * a.T + i),
+              "r"(sa(&full[G % kSB]))
+              : "memory");
+        }
       }
+      __syncwarp();
+      if (lane == 0) bar_arrive(&tab_empty[b]);
     }
   } else if (warp == kWarpMma) {
     // ---- MMA issuer: one wait and one commit per group, accumulator j % 2
