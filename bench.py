@@ -604,6 +604,13 @@ def run_serving(dev):
     # creations, cluster early in the stream
     arrived = np.array([x[2]["t_done"] - x[0] for x in res]) - t_base
     late = arrived >= 0.5 * arrived.max()
+    # where the latency goes: client (scheduled arrival -> submitted), queue
+    # (submitted -> admitted), service (admitted -> volume in host memory)
+    parts = {
+        "client": np.array([x[2]["t_submit"] - (x[2]["t_done"] - x[0]) for x in res]) * 1e3,
+        "queue": np.array([x[2]["t_start"] - x[2]["t_submit"] for x in res]) * 1e3,
+        "service": np.array([x[2]["t_done"] - x[2]["t_start"] for x in res]) * 1e3,
+    }
     span = max(x[2]["t_done"] for x in res) - t_base
     vt = sum(x[1] for x in res)
 
@@ -624,6 +631,9 @@ def run_serving(dev):
         "graph_replays_latency": pct(replay),
         "direct_runs_latency": pct(~replay),
         "second_half_latency": dict(pct(late), direct_runs=int((late & ~replay).sum())),
+        "latency_parts_ms": {k: {"p50": round(float(np.percentile(v, 50)), 3),
+                                 "p99": round(float(np.percentile(v, 99)), 3)}
+                             for k, v in parts.items()},
         "throughput_req_s": round(len(res) / span, 1),
         "value": round(vt / span / 1e9, 2),
         "unit": UNIT,
