@@ -418,4 +418,6 @@ cudaError_t launch_row_stage_w1024(const RowStageArgs &a, cudaStream_t s) {
   return cudaErrorInvalidValue;
 }
 
+GNC_MODULE_ANCHOR(w1024_kernels)
+
 }  // namespace gnc
