@@ -28,7 +28,7 @@ from .api import (  # noqa: F401
     reconstruct_ctf,
     reconstruct_file,
 )
-from .fbp import FbpDesc, FbpPlan, preload_kernels  # noqa: F401
+from .fbp import FbpDesc, FbpPlan  # noqa: F401
 from . import plot  # noqa: F401
 
 __version__ = "0.1.0"

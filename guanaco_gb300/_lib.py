@@ -153,7 +153,6 @@ SIGNATURES = {
                                   ctypes.POINTER(ctypes.c_uint64)]),
     "gnc_server_wait": (c_int, [c_void, ctypes.c_uint64, c_double,
                                 ctypes.POINTER(GncRequestInfo)]),
-    "gnc_preload_kernels": (c_int, []),
     "gnc_server_wait_any": (c_int, [c_void, c_double, ctypes.POINTER(ctypes.c_uint64),
                                     ctypes.POINTER(GncRequestInfo)]),
     "gnc_server_now": (c_double, [c_void]),

@@ -5,7 +5,6 @@
 // computed with the reference's float arithmetic; this file is compiled with
 // -ffp-contract=off so the host compiler forms no fused multiply-add on any
 // architecture.
-#include <cuda.h>
 #include <math.h>
 
 #include <algorithm>
@@ -500,64 +499,6 @@ int config_check(const gnc_config *c, const char *who) {
 }
 
 #undef GNC_CONFIG_REQUIRE
-
-GNC_MODULE_ANCHOR(api)
-
-
-// Driver entry points (CUDA 12.5 and later) of the library and kernel
-// management API, looked up at run time: the runtime links no driver library.
-typedef CUresult (*KernelGetLibraryFn)(CUlibrary *, CUkernel);
-typedef CUresult (*LibraryGetKernelCountFn)(unsigned int *, CUlibrary);
-typedef CUresult (*LibraryEnumerateKernelsFn)(CUkernel *, unsigned int, CUlibrary);
-typedef CUresult (*KernelGetFunctionFn)(CUfunction *, CUkernel);
-
-template <typename F>
-static bool driver_fn(const char *name, F *out) {
-  void *fn = nullptr;
-  cudaDriverEntryPointQueryResult q;
-  if (cudaGetDriverEntryPointByVersion(name, &fn, 12050, cudaEnableDefault, &q) != cudaSuccess ||
-      !fn || q != cudaDriverEntryPointSuccess)
-    return false;
-  *out = (F)fn;
-  return true;
-}
-
-cudaError_t load_module_kernels(const void *anchor) {
-  static KernelGetLibraryFn get_lib = nullptr;
-  static LibraryGetKernelCountFn count = nullptr;
-  static LibraryEnumerateKernelsFn enumerate = nullptr;
-  static KernelGetFunctionFn get_fn = nullptr;
-  if (!get_fn && !(driver_fn("cuKernelGetLibrary", &get_lib) &&
-                   driver_fn("cuLibraryGetKernelCount", &count) &&
-                   driver_fn("cuLibraryEnumerateKernels", &enumerate) &&
-                   driver_fn("cuKernelGetFunction", &get_fn)))
-    return cudaErrorNotSupported;
-  cudaKernel_t k = nullptr;
-  if (cudaError_t e = cudaGetKernel(&k, anchor)) return e;
-  CUlibrary lib = nullptr;
-  unsigned n = 0;
-  if (get_lib(&lib, (CUkernel)k) != CUDA_SUCCESS || count(&n, lib) != CUDA_SUCCESS)
-    return cudaErrorNotSupported;
-  std::vector<CUkernel> ks(n);
-  if (n && enumerate(ks.data(), n, lib) != CUDA_SUCCESS) return cudaErrorNotSupported;
-  for (CUkernel kk : ks) {  // a function handle in the current context loads the kernel there
-    CUfunction f = nullptr;
-    if (get_fn(&f, kk) != CUDA_SUCCESS) return cudaErrorNotSupported;
-  }
-  return cudaSuccess;
-}
-
-const void *module_anchor_b4096_kernels();
-const void *module_anchor_bp();
-const void *module_anchor_bp_fast();
-const void *module_anchor_bp_tc();
-const void *module_anchor_correct();
-const void *module_anchor_ctf();
-const void *module_anchor_noalloc();
-const void *module_anchor_pow2_kernels();
-const void *module_anchor_ramp();
-const void *module_anchor_w1024_kernels();
-const void *module_anchor_w512_kernels();
 
 }  // namespace gnc
 
@@ -1255,27 +1196,6 @@ int gnc_correct(const float *image, const float *ctf, float *rec, size_t xsize, 
   cudaError_t e2 = cudaStreamSynchronize(s);
   GNC_CUDA(e);
   GNC_CUDA(e2);
-  return GNC_OK;
-}
-
-int gnc_preload_kernels(void) {
-  const void *anchors[] = {gnc::module_anchor_api(),           gnc::module_anchor_b4096_kernels(),
-                           gnc::module_anchor_bp(),            gnc::module_anchor_bp_fast(),
-                           gnc::module_anchor_bp_tc(),         gnc::module_anchor_correct(),
-                           gnc::module_anchor_ctf(),           gnc::module_anchor_noalloc(),
-                           gnc::module_anchor_pow2_kernels(),  gnc::module_anchor_ramp(),
-                           gnc::module_anchor_w1024_kernels(), gnc::module_anchor_w512_kernels()};
-  for (const void *a : anchors) {
-    const cudaError_t e = gnc::load_module_kernels(a);
-    if (e == cudaErrorNotSupported) {
-      gnc::set_error("gnc_preload_kernels: the driver lacks the kernel enumeration API");
-      return GNC_ERR_UNSUPPORTED;
-    }
-    if (e != cudaSuccess) {
-      gnc::set_error(std::string("gnc_preload_kernels: ") + cudaGetErrorString(e));
-      return GNC_ERR_CUDA;
-    }
-  }
   return GNC_OK;
 }
 

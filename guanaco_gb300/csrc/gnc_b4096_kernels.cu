@@ -300,6 +300,4 @@ cudaError_t launch_row_stage_b4096(const RowStageArgs &a, cudaStream_t s) {
   return cudaErrorInvalidValue;
 }
 
-GNC_MODULE_ANCHOR(b4096_kernels)
-
 }  // namespace gnc

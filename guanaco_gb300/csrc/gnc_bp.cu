@@ -183,6 +183,4 @@ cudaError_t launch_backproject_slice(const SliceBpArgs &a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-GNC_MODULE_ANCHOR(bp)
-
 }  // namespace gnc

@@ -594,6 +594,4 @@ cudaError_t launch_backproject_fast(const BpArgs &a, cudaStream_t s) {
   return f16 ? launch_fast<4, 4, 4, true>(a, s) : launch_fast<4, 4, 4, false>(a, s);
 }
 
-GNC_MODULE_ANCHOR(bp_fast)
-
 }  // namespace gnc

@@ -742,6 +742,4 @@ cudaError_t launch_backproject_tc(const BpArgs &a, const TcMap &map, cudaStream_
   return map.rows == 256 ? launch_tc<256, 2, 8>(a, map, s) : launch_tc<128, 3, 12>(a, map, s);
 }
 
-GNC_MODULE_ANCHOR(bp_tc)
-
 }  // namespace gnc

@@ -300,18 +300,4 @@ __device__ __forceinline__ int slab_index(float x, float y, float sin_a, float c
   return k > D - 1 ? D - 1 : k;
 }
 
-// ---- loading this library's kernels before they are first launched --------
-// Every translation unit is its own device module, loaded lazily: the first
-// launch of each kernel loads it, which can stall the whole device for tens of
-// ms (seen as p99 spikes when a request stream first uses a kernel variant).
-// Each unit has an empty anchor kernel and exports its address
-// (GNC_MODULE_ANCHOR); load_module_kernels(anchor) loads every kernel of that
-// unit's module into the current context.
-namespace {
-__global__ void k_module_anchor() {}
-}  // namespace
-#define GNC_MODULE_ANCHOR(name) \
-  const void *module_anchor_##name() { return (const void *)&k_module_anchor; }
-cudaError_t load_module_kernels(const void *anchor);
-
 }  // namespace gnc

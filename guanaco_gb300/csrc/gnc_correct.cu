@@ -199,6 +199,4 @@ cudaError_t launch_column_flip(const float2 *spec, float2 *g, const int8_t *sign
   return cudaGetLastError();
 }
 
-GNC_MODULE_ANCHOR(correct)
-
 }  // namespace gnc

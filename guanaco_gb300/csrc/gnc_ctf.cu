@@ -317,8 +317,6 @@ __global__ void k_ctf_image(CtfImageArgs a, float *__restrict__ out) {
   }
 }
 
-GNC_MODULE_ANCHOR(ctf)
-
 }  // namespace gnc
 
 extern "C" {

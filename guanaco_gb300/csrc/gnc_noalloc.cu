@@ -125,8 +125,6 @@ __global__ void k_noalloc_ramp(float *rows, int nrows, int N, FftPlan plan, int 
 }
 
 }  // namespace
-GNC_MODULE_ANCHOR(noalloc)
-
 }  // namespace gnc
 
 using namespace gnc;

@@ -450,6 +450,4 @@ cudaError_t launch_row_stage_p2(const RowStageArgs &a, cudaStream_t s) {
   return cudaErrorInvalidValue;
 }
 
-GNC_MODULE_ANCHOR(pow2_kernels)
-
 }  // namespace gnc

@@ -214,6 +214,4 @@ cudaError_t launch_row_stage(const RowStageArgs &a, cudaStream_t s) {
   return cudaErrorInvalidValue;
 }
 
-GNC_MODULE_ANCHOR(ramp)
-
 }  // namespace gnc

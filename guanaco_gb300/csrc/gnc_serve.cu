@@ -511,9 +511,6 @@ int gnc_server_create(size_t budget_bytes, int slots, gnc_server **server) {
   }
   auto S = std::make_unique<gnc_server>();
   cudaGetDevice(&S->device);
-  // load the library's kernels now: a lazily loaded kernel's first launch
-  // inside the served stream stalls every request in flight
-  gnc_preload_kernels();
   S->budget = budget_bytes;
   S->slots.resize(slots);
   cudaError_t e = cudaStreamCreateWithFlags(&S->s_cap, cudaStreamNonBlocking);

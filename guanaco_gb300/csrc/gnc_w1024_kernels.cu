@@ -418,6 +418,4 @@ cudaError_t launch_row_stage_w1024(const RowStageArgs &a, cudaStream_t s) {
   return cudaErrorInvalidValue;
 }
 
-GNC_MODULE_ANCHOR(w1024_kernels)
-
 }  // namespace gnc

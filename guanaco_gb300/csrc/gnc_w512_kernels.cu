@@ -375,6 +375,4 @@ cudaError_t launch_row_stage_w512(const RowStageArgs &a, cudaStream_t s) {
   return cudaErrorInvalidValue;
 }
 
-GNC_MODULE_ANCHOR(w512_kernels)
-
 }  // namespace gnc

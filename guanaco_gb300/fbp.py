@@ -26,14 +26,6 @@ def _ptr(x):
     raise TypeError(f"cannot take a pointer of {type(x)!r}")
 
 
-def preload_kernels():
-    """Load every kernel of the library on the current device now rather than
-    at its first launch (gnc_preload_kernels): a lazily loaded kernel's first
-    launch can stall the device for tens of ms.  The request server does this
-    itself; call it once at startup before latency-sensitive plan use."""
-    _lib.check(_lib.load().gnc_preload_kernels())
-
-
 def _stream(stream):
     if stream is None:
         try:

@@ -268,14 +268,6 @@ GNC_API int gnc_fbp_backprojector(const gnc_fbp_plan *plan);
  * that barrier and the kernel ends normally.  polls = 0 (the default) turns it
  * off for plans created afterwards. */
 GNC_API int gnc_debug_wait_probe(unsigned polls);
-
-/* Loads every kernel of this library on the current device now, instead of
- * at its first launch (CUDA loads modules lazily by default, and a first
- * launch can stall the whole device for tens of ms).  gnc_server_create calls
- * it; a latency-sensitive caller of the plan API may call it once per device
- * at startup.  GNC_ERR_UNSUPPORTED if the driver lacks the kernel enumeration
- * API (CUDA 12.5 and later); the kernels then load on first use as before. */
-GNC_API int gnc_preload_kernels(void);
 /* Synchronises `stream` and reports (then clears) a device-side error of the
  * plan's kernels: every wait in them is bounded and records a timeout here
  * instead of hanging. */

@@ -176,12 +176,3 @@ def test_wait_any_reports_each_request_once_in_finishing_order(G):
     assert first["status"] == 0
     for rid, (out, want) in outs.items():
         np.testing.assert_array_equal(out, want)
-
-
-def test_preload_kernels_loads_the_library(G):
-    """gnc_preload_kernels (called by gnc_server_create) loads every kernel of
-    the library on the current device; a plan run afterwards is unaffected."""
-    G.preload_kernels()
-    G.preload_kernels()  # idempotent
-    args, kw, proj = _request(G, 64, 11, 3, "f32", seed=300)
-    np.testing.assert_array_equal(_alone(G, args, kw, proj), _alone(G, args, kw, proj))
