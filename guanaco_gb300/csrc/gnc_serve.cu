@@ -187,9 +187,10 @@ Cached *find_idle(gnc_server *S, const std::string &key) {
   return nullptr;
 }
 
-bool being_built(gnc_server *S, const std::string &key) {
+// Whether the shape has a plan (running a request, or being built).
+bool has_plan(gnc_server *S, const std::string &key) {
   for (auto &c : S->cache)
-    if (!c->ready && c->key == key) return true;
+    if (c->key == key) return true;
   return false;
 }
 
@@ -343,8 +344,11 @@ void admit(gnc_server *S, std::unique_lock<std::mutex> &lk) {
       if (qi > 0 && S->head_skips >= kMaxSkips) break;
       Request *q = S->queue[qi];
       c = find_idle(S, q->key);
-      // a shape whose plan the builder is making waits for it (no second copy)
-      if (!c && being_built(S, q->key)) continue;
+      // a shape whose plan is busy or being built waits for it rather than
+      // building a second copy: under load a copy per overlapping request
+      // multiplied the builds (each a direct run and a capture on the same
+      // GPU), which slowed service and so made more requests overlap
+      if (!c && has_plan(S, q->key)) continue;
       if (c || S->used - idle + q->bytes <= S->budget) {
         r = q;
         break;
