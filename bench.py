@@ -571,6 +571,25 @@ def drive_stream(srv, stream, descs, inputs, pools, t_base):
     return done
 
 
+def host_link_gbs(dev, nbytes=256 << 20):
+    """Host <-> device copy rate (GB/s, down and up) of one page-locked buffer:
+    the link every served request's input and volume cross."""
+    import torch
+
+    h = torch.empty(nbytes // 4, dtype=torch.float32).pin_memory()
+    d = torch.empty(nbytes // 4, dtype=torch.float32, device=dev)
+    rates = []
+    for src, dst in ((d, h), (h, d)):
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(4):
+            dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        rates.append(round(4 * nbytes / (time.perf_counter() - t0) / 1e9, 1))
+    return rates
+
+
 def run_serving(dev):
     """The mixed serving stream through the request server: a burst of
     SERVE['burst'] requests, run once to create its shapes' plans and graphs and
@@ -595,8 +614,13 @@ def run_serving(dev):
         rate = cfg["load"] * capacity
         stream = synthetic.request_stream(cfg["requests"], rate, seed=cfg["seed"])
         descs = [serving_desc(r) for r in stream]
+        link_before = host_link_gbs(dev)
+        clocks = ClockSampler(dev.index)
+        clocks.start()
         t_base = srv.now() + 0.05
         res = drive_stream(srv, stream, descs, inputs, pools, t_base)
+        clk = clocks.stop()
+        link_after = host_link_gbs(dev)
         stats = srv.stats()
     lat = np.array([x[0] for x in res]) * 1e3
     replay = np.array([bool(x[2]["graph"]) for x in res])
@@ -631,6 +655,8 @@ def run_serving(dev):
         "graph_replays_latency": pct(replay),
         "direct_runs_latency": pct(~replay),
         "second_half_latency": dict(pct(late), direct_runs=int((late & ~replay).sum())),
+        "clocks": clk,
+        "host_link_gbs": {"down_up_before": link_before, "down_up_after": link_after},
         "latency_parts_ms": {k: {"p50": round(float(np.percentile(v, 50)), 3),
                                  "p99": round(float(np.percentile(v, 99)), 3)}
                              for k, v in parts.items()},
