@@ -53,12 +53,14 @@
 // one lane per copy 1.60 ms.  What bounds the group loop is the window copies:
 // without them (a timing-only variant, wrong volumes, every wait kept) it
 // takes 1.10 ms, without the weight stores 1.61 ms, and clock stamps show the
-// MMA thread waiting some 700 of a group's 1400 cycles for windows; a 256-row
-// box of 64-byte rows keeps the copy engine busy about 300 cycles, one row per
-// cycle.  Halving the bytes per voxel (16 x 16 tiles, two MMA groups sharing
-// 128-row windows) and a deeper window ring (copies four groups ahead) did not
-// change the time, so the engine's rate for narrow rows, not the bytes or the
-// latency, is the bound.  Prefetching the windows of later tilts into
+// MMA thread waiting some 700 of a group's 1400 cycles for windows; a copy
+// (one box of 32 pixels x 256 rows) keeps the copy engine busy about 300
+// cycles.  Boxes of 128 rows with the same number of copies per group (16 x 16
+// tiles, two MMA groups sharing each window: half the bytes per voxel) and a
+// deeper window ring (copies four groups ahead) did not change the time, and
+// 16-byte cp.async copies from three warps instead of the tensor copies were
+// three times slower, so the number of tensor copies per group, not their bytes
+// or their latency, is the bound.  Prefetching the windows of later tilts into
 // L2 made the kernel 25 % slower (the prefetches compete with the loads).
 // Every wait is bounded and records a timeout in the plan's error word; after
 // one timeout the block's remaining waits return at once.
