@@ -615,12 +615,14 @@ def run_serving(dev):
         stream = synthetic.request_stream(cfg["requests"], rate, seed=cfg["seed"])
         descs = [serving_desc(r) for r in stream]
         link_before = host_link_gbs(dev)
+        load_before = os.getloadavg()
         clocks = ClockSampler(dev.index)
         clocks.start()
         t_base = srv.now() + 0.05
         res = drive_stream(srv, stream, descs, inputs, pools, t_base)
         clk = clocks.stop()
         link_after = host_link_gbs(dev)
+        load_after = os.getloadavg()
         stats = srv.stats()
     lat = np.array([x[0] for x in res]) * 1e3
     replay = np.array([bool(x[2]["graph"]) for x in res])
@@ -657,6 +659,10 @@ def run_serving(dev):
         "second_half_latency": dict(pct(late), direct_runs=int((late & ~replay).sum())),
         "clocks": clk,
         "host_link_gbs": {"down_up_before": link_before, "down_up_after": link_after},
+        # the server's scheduler, builder and completion callbacks are host
+        # threads: the host's load average (1, 5, 15 min) and its CPU count
+        "host_load": {"before": [round(x, 2) for x in load_before],
+                      "after": [round(x, 2) for x in load_after], "cpus": os.cpu_count()},
         "latency_parts_ms": {k: {"p50": round(float(np.percentile(v, 50)), 3),
                                  "p99": round(float(np.percentile(v, 99)), 3)}
                              for k, v in parts.items()},
