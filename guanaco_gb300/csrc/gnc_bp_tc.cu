@@ -274,7 +274,7 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
   // threads have read it.  tab_full[b]: table buffer b is written; tab_empty[b]:
   // the producer, the MMA issuer and the builders are done with it.
   __shared__ __align__(8) u64 full[kSB], empty[kSB], acc_full[2], acc_empty[2], tab_full[2],
-      tab_empty[2], done_bar;
+      tab_empty[2], done_bar, probe_bar;
   __shared__ unsigned tmem_base;
   __shared__ int s_e0;
   __shared__ volatile int s_abort;
@@ -313,6 +313,7 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
       bar_init(&tab_empty[b], kBuilders + 2);
     }
     bar_init(&done_bar, 1);
+    bar_init(&probe_bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     s_e0 = 127;
     s_abort = 0;
@@ -601,6 +602,14 @@ k_bp_tc(BpArgs a, const __grid_constant__ CUtensorMap map) {
   }
   tc_fence_before();
   __syncthreads();
+  // Test hook (gnc_debug_wait_probe): after the block's work, one thread arms
+  // a spare barrier for 16 bytes that no copy delivers and waits on it with the
+  // probe's poll limit, so the wait gives up and sets the error word as a lost
+  // copy would; nothing is in flight on that barrier.
+  if (a.wait_probe && tid == 0 && blockIdx.x == 0) {
+    bar_expect_tx(&probe_bar, 16);
+    bar_wait(&probe_bar, 0, a.wait_probe, a.err, &s_abort);
+  }
   if (warp == kWarpMma)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"((unsigned)P::kTmemCols));

@@ -1,13 +1,13 @@
 """Failure detection of the bounded device waits, without a GPU fault.
 
-Every mbarrier wait in the fast backprojector gives up after a bounded number
-of polls and records the timeout in the plan's device error word, which
-gnc_fbp_check and the request server report.  gnc_debug_wait_probe makes the
-give-up happen on purpose: each fast backprojection launch of a plan created
-while it is on arms a spare mbarrier for 16 bytes that no copy ever delivers
-and waits on it for a short, bounded number of polls.  Nothing is in flight on
-that barrier, so the kernel ends normally and the context stays usable; the
-tests check the reported status, that it clears, that the volume is unchanged
+Every mbarrier wait in the fast and the tensor-core backprojectors gives up
+after a bounded number of polls and records the timeout in the plan's device
+error word, which gnc_fbp_check and the request server report.
+gnc_debug_wait_probe makes the give-up happen on purpose: each backprojection
+launch of a plan created while it is on arms a spare mbarrier for 16 bytes that
+no copy ever delivers and waits on it for a short, bounded number of polls.
+Nothing is in flight on that barrier, so the kernel ends normally and the
+context stays usable; the tests check the reported status, that it clears, that the volume is unchanged
 and that plans created after the probe is turned off report nothing.
 """
 import numpy as np
@@ -45,12 +45,15 @@ def _series(G, T=9, n=128, Z=48, D=2, staging="f32", df=20000.0, seed=3):
     return (T, n, n, ang), desc, proj
 
 
-@pytest.mark.parametrize("staging", ["f32", "f16"])
+@pytest.mark.parametrize("staging", ["f32", "f16", "f16t"])
 def test_wait_that_gives_up_is_reported_by_check(env, staging):
     torch, G, _lib, L = env
     args, desc, proj = _series(G, staging=staging)
     clean = G.FbpPlan(*args, **desc)
-    assert clean.backprojector > 0, "the probe lives in the fast backprojector"
+    # the probe lives in the fast and the tensor-core backprojectors
+    assert clean.backprojector > 0
+    if staging == "f16t":
+        assert clean.backprojector == 16
     want = clean.execute_host(proj)
     clean.check()
     clean.close()
