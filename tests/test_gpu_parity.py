@@ -343,11 +343,16 @@ def test_fast_backprojector_tilt_chunks(torch, oracle, staging, D, variant):
 # and the exact backprojector on the same FP16 rows closely (they differ only
 # in the FP16 interpolation weights and the summation order).  Shapes: volume
 # edges that cut tiles (X, Z not multiples of 16 and 8, rows not a multiple
-# of 128), several slabs per tile, one slab, 300 tilts, a 1024-pixel detector.
+# of 128), several slabs per tile, one slab, 300 tilts, a 1024-pixel detector;
+# and 1-3 tilts over some 16 tiles per block, where a tile has only one or two
+# slab slots, so a group's ring slots were last used several tiles back (the
+# wait falls back to the last group two tiles back).
 @pytest.mark.parametrize("T,H,W,Z,X,D", [(17, 12, 48, 40, 48, 5), (17, 12, 64, 40, 64, 6),
                                          (9, 130, 64, 37, 64, 3),
                                          (300, 6, 128, 48, 128, 3), (21, 16, 64, 64, 64, 1),
-                                         (13, 4, 1024, 300, 1024, 10), (11, 20, 96, 21, 53, 4)])
+                                         (13, 4, 1024, 300, 1024, 10), (11, 20, 96, 21, 53, 4),
+                                         (1, 4, 1024, 300, 1024, 3), (2, 4, 1024, 300, 1024, 3),
+                                         (3, 4, 512, 300, 512, 2)])
 def test_tensor_core_backprojector(torch, oracle, T, H, W, Z, X, D):
     import guanaco_gb300 as G
 
