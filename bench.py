@@ -36,8 +36,9 @@ import numpy as np
 
 # Load every CUDA kernel when the context is created rather than at its first
 # launch, as a latency-sensitive service would: a lazily loaded kernel's first
-# launch inside the serving stream stalled every request in flight (p99 tails
-# of 100+ ms in some runs).  A caller's own setting wins.
+# launch inside the serving stream can hold up the requests in flight (the
+# stream's p99 tail of about 100 ms appeared in fewer runs with eager loading).
+# A caller's own setting wins.
 os.environ.setdefault("CUDA_MODULE_LOADING", "EAGER")
 
 REPO = os.path.dirname(os.path.abspath(__file__))
